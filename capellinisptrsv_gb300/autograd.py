@@ -1,0 +1,54 @@
+"""Differentiable sparse triangular solve: x = L^{-1} b as a torch.autograd.Function.
+
+Forward runs the row-driven sync-free solve.  Backward is hand-written: one
+column-driven sync-free sweep over the SAME CSR arrays solves L^T y = g
+(grad_b = y; no transpose is built) and, fused into it, writes
+grad_val[k] = -sum_r y[row_k, r] * x[col_k, r] for every stored entry k.
+"""
+from __future__ import annotations
+
+import torch
+
+from .solver import TriangularSolver
+
+__all__ = ["SparseTriangularSolve", "sptrsv", "DifferentiableTriangular"]
+
+
+class SparseTriangularSolve(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, val: torch.Tensor, b: torch.Tensor, solver: TriangularSolver):
+        solver.bind_values(val.detach())
+        x = solver.solve(b.detach())
+        ctx.solver = solver
+        ctx.save_for_backward(val, x)
+        return x
+
+    @staticmethod
+    def backward(ctx, gx: torch.Tensor):
+        val, x = ctx.saved_tensors
+        solver: TriangularSolver = ctx.solver
+        solver.bind_values(val.detach())
+        gx = gx.contiguous()
+        need_val, need_b = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+        if need_val:
+            y, gval = solver.solve_transpose_grad(gx, x)
+        else:
+            y, gval = solver.solve_transpose(gx), None
+        return gval, (y if need_b else None), None
+
+
+def sptrsv(solver: TriangularSolver, val: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """x = L(val)^{-1} b, differentiable in val and b."""
+    return SparseTriangularSolve.apply(val, b, solver)
+
+
+class DifferentiableTriangular(torch.nn.Module):
+    """A lower-triangular CSR operator with learnable values (a torch.nn.Parameter)."""
+
+    def __init__(self, rowptr: torch.Tensor, colidx: torch.Tensor, val: torch.Tensor, **solver_kwargs):
+        super().__init__()
+        self.val = torch.nn.Parameter(val.detach().clone())
+        self.solver = TriangularSolver(rowptr, colidx, self.val.detach(), **solver_kwargs)
+
+    def forward(self, b: torch.Tensor) -> torch.Tensor:
+        return sptrsv(self.solver, self.val, b)

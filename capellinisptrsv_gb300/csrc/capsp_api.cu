@@ -1,0 +1,1037 @@
+// Native C-ABI of libcapsp: handle lifetime, analysis, solve dispatch,
+// autotuning and CUDA-graph replay.  All device work is stream-ordered on the
+// caller's stream; the only synchronising calls are capsp_analyse,
+// capsp_set_values, capsp_status_sync, capsp_solve_host and capsp_autotune.
+#include "capsp.h"
+#include "capsp_internal.h"
+
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+using namespace capsp;
+
+// ---------------------------------------------------------------------------
+// error reporting
+// ---------------------------------------------------------------------------
+
+static thread_local std::string g_last_error;
+
+static capsp_status_t fail(capsp_status_t st, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return st;
+}
+
+#define CAPSP_CUDA(call)                                                                       \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(e_ == cudaErrorMemoryAllocation ? CAPSP_ERR_OOM : CAPSP_ERR_CUDA,      \
+                        "%s failed: %s", #call, cudaGetErrorString(e_));                       \
+    } while (0)
+
+#define CAPSP_TRY(expr)                                                                        \
+    do {                                                                                       \
+        capsp_status_t s_ = (expr);                                                            \
+        if (s_ != CAPSP_OK)                                                                    \
+            return s_;                                                                         \
+    } while (0)
+
+extern "C" const char *capsp_last_error(void) { return g_last_error.c_str(); }
+
+// ---------------------------------------------------------------------------
+// handle
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct Tuning {
+    int kind;   // kRowWrtFst / kRowTwoPart / kRowMix (row path); ignored on the column path
+    int R;      // rows per thread
+    int block;  // threads per block
+    int bps;    // blocks per SM (0: occupancy maximum)
+    int border; // mix border
+};
+
+struct MixTable {
+    int *d = nullptr;
+    int len = 0;
+    int border = INT_MIN;
+    double wo = 0.0, eo = 0.0;
+};
+
+typedef std::tuple<const void *, void *, int, int64_t, void *, int> GraphKey;
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev)
+            cudaSetDevice(dev);
+        else
+            prev = -1;
+    }
+    ~DeviceGuard()
+    {
+        if (prev >= 0)
+            cudaSetDevice(prev);
+    }
+};
+
+}  // namespace
+
+struct capsp_handle_s {
+    int device = 0;
+    int num_sms = 1;
+    int n = 0, nnz = 0, dtype = 0, format = 0, uplo = 0;
+    unsigned flags = 0;
+    size_t vbytes = 8;
+    int *d_ptr = nullptr;
+    int *d_idx = nullptr;
+    void *d_val = nullptr;
+    bool own_struct = false;  // d_ptr / d_idx allocated here
+    bool own_val = false;     // d_val allocated here
+    std::vector<int> h_ptr;
+    void *d_inv = nullptr;
+    unsigned *d_ticket = nullptr;  // [64] ticket counters followed by the error word
+    int *d_err = nullptr;          // [4]
+    int *d_indeg = nullptr;
+    int *d_arrived = nullptr;
+    void *d_left = nullptr;
+    int left_cap = 0;  // right-hand sides the left_sum scratch holds
+    std::map<int, MixTable> mix;
+    int alg = CAPSP_ALG_AUTO;
+    int border = 10;
+    Tuning tune = {kRowWrtFst, 2, 256, 0, 10};
+    bool tune_explicit = false;
+    std::map<int, Tuning> tuned;
+    WaitCfg wait = {10000000000ull, 1u << 30, 1024u};
+    int stuck_row = -1;
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    void *d_stage = nullptr;
+    size_t stage_bytes = 0;
+    cudaStream_t stage_stream = nullptr;
+    double analyse_ms = 0.0;
+    bool profiling = false;
+    cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;
+    int nsys = 0;
+    std::vector<int> sys_rowoff;
+    std::recursive_mutex mu;
+};
+
+static bool diag_last_of(int format, int uplo) { return (format == CAPSP_FMT_CSR) == (uplo == CAPSP_LOWER); }
+
+static void free_handle(capsp_handle_t h)
+{
+    if (!h)
+        return;
+    DeviceGuard g(h->device);
+    for (auto &kv : h->graphs)
+        cudaGraphExecDestroy(kv.second);
+    for (auto &kv : h->mix)
+        cudaFree(kv.second.d);
+    if (h->own_struct) {
+        cudaFree(h->d_ptr);
+        cudaFree(h->d_idx);
+    }
+    if (h->own_val)
+        cudaFree(h->d_val);
+    cudaFree(h->d_inv);
+    cudaFree(h->d_ticket);
+    cudaFree(h->d_indeg);
+    cudaFree(h->d_arrived);
+    cudaFree(h->d_left);
+    cudaFree(h->d_stage);
+    if (h->stage_stream)
+        cudaStreamDestroy(h->stage_stream);
+    if (h->ev_k0)
+        cudaEventDestroy(h->ev_k0);
+    if (h->ev_k1)
+        cudaEventDestroy(h->ev_k1);
+    delete h;
+}
+
+// refresh 1/diag from the handle's current values; synchronous
+static capsp_status_t refresh_inv_diag(capsp_handle_t h)
+{
+    int *d_bad = nullptr;
+    CAPSP_CUDA(cudaMalloc(&d_bad, sizeof(int)));
+    const int big = INT_MAX;
+    cudaError_t e = cudaMemcpy(d_bad, &big, sizeof(int), cudaMemcpyHostToDevice);
+    const int dl = diag_last_of(h->format, h->uplo);
+    if (e == cudaSuccess) {
+        if (h->dtype == CAPSP_R_64F)
+            e = launch_inv_diag<double>(h->d_ptr, (const double *)h->d_val, (double *)h->d_inv, h->n,
+                                        dl, d_bad, 0);
+        else
+            e = launch_inv_diag<float>(h->d_ptr, (const float *)h->d_val, (float *)h->d_inv, h->n, dl,
+                                       d_bad, 0);
+    }
+    int bad = INT_MAX;
+    if (e == cudaSuccess)
+        e = cudaMemcpy(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d_bad);
+    if (e != cudaSuccess)
+        return fail(CAPSP_ERR_CUDA, "computing 1/diag failed: %s", cudaGetErrorString(e));
+    if (bad != INT_MAX)
+        return fail(CAPSP_ERR_INVALID, "diagonal entry of row/column %d is zero or not finite", bad);
+    return CAPSP_OK;
+}
+
+extern "C" capsp_status_t capsp_device_sms(int *num_sms)
+{
+    if (!num_sms)
+        return fail(CAPSP_ERR_INVALID, "num_sms is NULL");
+    int dev = 0;
+    CAPSP_CUDA(cudaGetDevice(&dev));
+    CAPSP_CUDA(cudaDeviceGetAttribute(num_sms, cudaDevAttrMultiProcessorCount, dev));
+    return CAPSP_OK;
+}
+
+extern "C" capsp_status_t capsp_analyse(int n, int nnz, const int *ptr, const int *idx,
+                                        const void *val, int dtype, int format, int uplo,
+                                        unsigned flags, capsp_handle_t *out)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    if (!out)
+        return fail(CAPSP_ERR_INVALID, "out handle pointer is NULL");
+    *out = nullptr;
+    if (!ptr || !idx || !val)
+        return fail(CAPSP_ERR_INVALID, "ptr, idx and val must be non-NULL");
+    if (n < 1 || nnz < n)
+        return fail(CAPSP_ERR_INVALID, "need n >= 1 and nnz >= n (got n=%d, nnz=%d)", n, nnz);
+    if (dtype != CAPSP_R_64F && dtype != CAPSP_R_32F)
+        return fail(CAPSP_ERR_INVALID, "unknown dtype %d", dtype);
+    if (format != CAPSP_FMT_CSR && format != CAPSP_FMT_CSC)
+        return fail(CAPSP_ERR_INVALID, "unknown format %d", format);
+    if (uplo != CAPSP_LOWER && uplo != CAPSP_UPPER)
+        return fail(CAPSP_ERR_INVALID, "unknown uplo %d", uplo);
+
+    capsp_handle_t h = new (std::nothrow) capsp_handle_s();
+    if (!h)
+        return fail(CAPSP_ERR_OOM, "host allocation of the handle failed");
+    h->n = n;
+    h->nnz = nnz;
+    h->dtype = dtype;
+    h->format = format;
+    h->uplo = uplo;
+    h->flags = flags;
+    h->vbytes = dtype == CAPSP_R_64F ? 8 : 4;
+    capsp_status_t st = CAPSP_OK;
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+    if (e != cudaSuccess) {
+        free_handle(h);
+        return fail(CAPSP_ERR_CUDA, "no usable CUDA device: %s", cudaGetErrorString(e));
+    }
+    const int dl = diag_last_of(format, uplo);
+    h->h_ptr.resize((size_t)n + 1);
+
+    if (!(flags & CAPSP_DEVICE_POINTERS)) {
+        if (!(flags & CAPSP_SKIP_VALIDATION)) {
+            char msg[256];
+            if (capsp_validate(n, nnz, ptr, idx, format, uplo, msg, sizeof(msg)) != 0) {
+                free_handle(h);
+                return fail(CAPSP_ERR_INVALID, "invalid matrix: %s", msg);
+            }
+        }
+        memcpy(h->h_ptr.data(), ptr, sizeof(int) * ((size_t)n + 1));
+        h->own_struct = h->own_val = true;
+        e = cudaMalloc(&h->d_ptr, sizeof(int) * ((size_t)n + 1));
+        if (e == cudaSuccess)
+            e = cudaMalloc(&h->d_idx, sizeof(int) * (size_t)nnz);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&h->d_val, h->vbytes * (size_t)nnz);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(h->d_ptr, ptr, sizeof(int) * ((size_t)n + 1), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(h->d_idx, idx, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(h->d_val, val, h->vbytes * (size_t)nnz, cudaMemcpyHostToDevice);
+    } else {
+        h->d_ptr = const_cast<int *>(ptr);
+        h->d_idx = const_cast<int *>(idx);
+        h->d_val = const_cast<void *>(val);
+        e = cudaMemcpy(h->h_ptr.data(), ptr, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && !(flags & CAPSP_SKIP_VALIDATION)) {
+            int *d_bad = nullptr;
+            e = cudaMalloc(&d_bad, sizeof(int));
+            const int big = INT_MAX;
+            int bad = INT_MAX;
+            if (e == cudaSuccess)
+                e = cudaMemcpy(d_bad, &big, sizeof(int), cudaMemcpyHostToDevice);
+            if (e == cudaSuccess)
+                e = launch_validate(h->d_ptr, h->d_idx, n, nnz, dl, d_bad, 0);
+            if (e == cudaSuccess)
+                e = cudaMemcpy(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost);
+            cudaFree(d_bad);
+            if (e == cudaSuccess && (bad != INT_MAX || h->h_ptr[0] != 0 || h->h_ptr[n] != nnz)) {
+                free_handle(h);
+                return fail(CAPSP_ERR_INVALID,
+                            "invalid matrix: row/column %d has a missing or misplaced diagonal, an "
+                            "index on the wrong side of it, or an out-of-order pointer",
+                            bad == INT_MAX ? 0 : bad);
+            }
+        }
+    }
+    if (e == cudaSuccess)
+        e = cudaMalloc(&h->d_inv, h->vbytes * (size_t)n);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&h->d_ticket, sizeof(unsigned) * 64 + sizeof(int) * 4);
+    if (e == cudaSuccess)
+        e = cudaMemset(h->d_ticket, 0, sizeof(unsigned) * 64 + sizeof(int) * 4);
+    if (e != cudaSuccess) {
+        free_handle(h);
+        return fail(e == cudaErrorMemoryAllocation ? CAPSP_ERR_OOM : CAPSP_ERR_CUDA,
+                    "analysis failed: %s", cudaGetErrorString(e));
+    }
+    h->d_err = reinterpret_cast<int *>(h->d_ticket + 64);
+    st = refresh_inv_diag(h);
+    if (st != CAPSP_OK) {
+        free_handle(h);
+        return st;
+    }
+    h->analyse_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    *out = h;
+    return CAPSP_OK;
+}
+
+extern "C" capsp_status_t capsp_batched_create(int nsys, const int *sys_rowoff, int n, int nnz,
+                                               const int *ptr, const int *idx, const void *val,
+                                               int dtype, unsigned flags, capsp_handle_t *out)
+{
+    if (!out)
+        return fail(CAPSP_ERR_INVALID, "out handle pointer is NULL");
+    *out = nullptr;
+    if (nsys < 1 || !sys_rowoff)
+        return fail(CAPSP_ERR_INVALID, "need nsys >= 1 and a system row-offset table");
+    if (sys_rowoff[0] != 0 || sys_rowoff[nsys] != n)
+        return fail(CAPSP_ERR_INVALID, "sys_rowoff must start at 0 and end at n=%d", n);
+    for (int s = 0; s < nsys; ++s)
+        if (sys_rowoff[s + 1] <= sys_rowoff[s])
+            return fail(CAPSP_ERR_INVALID, "system %d is empty or out of order", s);
+    if (!(flags & CAPSP_DEVICE_POINTERS) && !(flags & CAPSP_SKIP_VALIDATION) && ptr && idx) {
+        // every entry must stay inside its own system's diagonal block
+        for (int s = 0; s < nsys; ++s)
+            for (int i = sys_rowoff[s]; i < sys_rowoff[s + 1]; ++i)
+                for (int j = ptr[i]; j < ptr[i + 1]; ++j)
+                    if (idx[j] < sys_rowoff[s] || idx[j] > i)
+                        return fail(CAPSP_ERR_INVALID,
+                                    "row %d of system %d references column %d outside its block", i,
+                                    s, idx[j]);
+    }
+    capsp_handle_t h = nullptr;
+    CAPSP_TRY(capsp_analyse(n, nnz, ptr, idx, val, dtype, CAPSP_FMT_CSR, CAPSP_LOWER, flags, &h));
+    h->nsys = nsys;
+    h->sys_rowoff.assign(sys_rowoff, sys_rowoff + nsys + 1);
+    *out = h;
+    return CAPSP_OK;
+}
+
+extern "C" capsp_status_t capsp_destroy(capsp_handle_t h)
+{
+    free_handle(h);
+    return CAPSP_OK;
+}
+
+extern "C" capsp_status_t capsp_set_values(capsp_handle_t h, const void *val)
+{
+    if (!h || !val)
+        return fail(CAPSP_ERR_INVALID, "handle and val must be non-NULL");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    if (h->flags & CAPSP_DEVICE_POINTERS) {
+        h->d_val = const_cast<void *>(val);
+    } else {
+        CAPSP_CUDA(cudaMemcpy(h->d_val, val, h->vbytes * (size_t)h->nnz, cudaMemcpyHostToDevice));
+    }
+    return refresh_inv_diag(h);
+}
+
+extern "C" capsp_status_t capsp_set_algorithm(capsp_handle_t h, int algorithm)
+{
+    if (!h)
+        return fail(CAPSP_ERR_INVALID, "handle is NULL");
+    if (algorithm < CAPSP_ALG_AUTO || algorithm > CAPSP_ALG_SYNCFREE_CSC)
+        return fail(CAPSP_ERR_INVALID, "unknown algorithm %d", algorithm);
+    if (algorithm == CAPSP_ALG_SYNCFREE_CSC && h->format != CAPSP_FMT_CSC)
+        return fail(CAPSP_ERR_UNSUPPORTED,
+                    "the warp-per-column kernel solves CSC handles; build the CSC with "
+                    "matrix_transposition and analyse it with CAPSP_FMT_CSC");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    h->alg = algorithm;
+    h->tuned.clear();
+    return CAPSP_OK;
+}
+
+extern "C" capsp_status_t capsp_set_mix_border(capsp_handle_t h, int border)
+{
+    if (!h)
+        return fail(CAPSP_ERR_INVALID, "handle is NULL");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    h->border = border;
+    h->tune.border = border;
+    h->tuned.clear();
+    return CAPSP_OK;
+}
+
+extern "C" capsp_status_t capsp_set_tuning(capsp_handle_t h, int rows_per_thread, int block_threads,
+                                           int blocks_per_sm)
+{
+    if (!h)
+        return fail(CAPSP_ERR_INVALID, "handle is NULL");
+    if (rows_per_thread != 1 && rows_per_thread != 2 && rows_per_thread != 4)
+        return fail(CAPSP_ERR_INVALID, "rows_per_thread must be 1, 2 or 4");
+    if (block_threads < 64 || block_threads > 512 || block_threads % 32)
+        return fail(CAPSP_ERR_INVALID, "block_threads must be a multiple of 32 in [64, 512]");
+    if (blocks_per_sm < 0)
+        return fail(CAPSP_ERR_INVALID, "blocks_per_sm must be >= 0");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    h->tune.R = rows_per_thread;
+    h->tune.block = block_threads;
+    h->tune.bps = blocks_per_sm;
+    h->tune_explicit = true;
+    h->tuned.clear();
+    return CAPSP_OK;
+}
+
+extern "C" capsp_status_t capsp_set_timeout(capsp_handle_t h, uint64_t timeout_ns)
+{
+    if (!h || timeout_ns == 0)
+        return fail(CAPSP_ERR_INVALID, "need a handle and a positive timeout");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    h->wait.timeout_ns = timeout_ns;
+    return CAPSP_OK;
+}
+
+extern "C" capsp_status_t capsp_debug_set_stuck_row(capsp_handle_t h, int row, uint64_t timeout_ns)
+{
+    if (!h || row < -1 || row >= h->n)
+        return fail(CAPSP_ERR_INVALID, "need a handle and a row in [-1, n)");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    h->stuck_row = row;
+    if (timeout_ns)
+        h->wait.timeout_ns = timeout_ns;
+    return CAPSP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// lazily built analysis products (never called while a stream is captured
+// for the first time: prepare() runs them before capture)
+// ---------------------------------------------------------------------------
+
+// rows per mix group for a launch with nrhs right-hand sides
+static int group_rows_for(int nrhs) { return 32 / lanes_for_rhs(nrhs < 32 ? nrhs : 32); }
+
+// row path view: CSR handles solve their rows; CSC handles read their columns
+// as rows of the transpose
+static int row_view_upper(capsp_handle_t h, bool transpose)
+{
+    return transpose ? (h->uplo == CAPSP_LOWER) : (h->uplo == CAPSP_UPPER);
+}
+
+static capsp_status_t ensure_mix(capsp_handle_t h, int group_rows, int border, bool view_upper,
+                                 MixTable **out)
+{
+    MixTable &mt = h->mix[group_rows];
+    if (mt.d == nullptr || mt.border != border) {
+        std::vector<int> table((size_t)h->n + 2);
+        double wo = 0.0, eo = 0.0;
+        const int len = capsp_mix_table(h->n, h->h_ptr.data(), view_upper ? 1 : 0, group_rows,
+                                        border, table.data(), &wo, &eo);
+        if (mt.d == nullptr)
+            CAPSP_CUDA(cudaMalloc(&mt.d, sizeof(int) * ((size_t)h->n + 2)));
+        CAPSP_CUDA(cudaMemcpy(mt.d, table.data(), sizeof(int) * (size_t)len, cudaMemcpyHostToDevice));
+        mt.len = len;
+        mt.border = border;
+        mt.wo = wo;
+        mt.eo = eo;
+    }
+    *out = &mt;
+    return CAPSP_OK;
+}
+
+static capsp_status_t ensure_column_scratch(capsp_handle_t h, int nrhs)
+{
+    if (!h->d_indeg) {
+        CAPSP_CUDA(cudaMalloc(&h->d_indeg, sizeof(int) * (size_t)h->n));
+        CAPSP_CUDA(cudaMemset(h->d_indeg, 0, sizeof(int) * (size_t)h->n));
+        CAPSP_CUDA(launch_histogram(h->d_idx, h->nnz, h->d_indeg, 0));
+        CAPSP_CUDA(cudaDeviceSynchronize());
+    }
+    if (!h->d_arrived)
+        CAPSP_CUDA(cudaMalloc(&h->d_arrived, sizeof(int) * (size_t)h->n));
+    const int want = nrhs < 32 ? nrhs : 32;
+    if (h->left_cap < want) {
+        cudaFree(h->d_left);
+        h->d_left = nullptr;
+        h->left_cap = 0;
+        CAPSP_CUDA(cudaMalloc(&h->d_left, h->vbytes * (size_t)h->n * (size_t)want));
+        h->left_cap = want;
+    }
+    return CAPSP_OK;
+}
+
+static Tuning current_tuning(capsp_handle_t h, int nrhs)
+{
+    auto it = h->tuned.find(nrhs);
+    if (it != h->tuned.end())
+        return it->second;
+    Tuning t = h->tune;
+    t.border = h->border;
+    switch (h->alg) {
+    case CAPSP_ALG_TWOPART: t.kind = kRowTwoPart; break;
+    case CAPSP_ALG_MIX: t.kind = kRowMix; break;
+    case CAPSP_ALG_WRTFST: t.kind = kRowWrtFst; break;
+    default: t.kind = -1; break;  // AUTO: decided from the mix table
+    }
+    return t;
+}
+
+// ---------------------------------------------------------------------------
+// enqueue paths
+// ---------------------------------------------------------------------------
+
+template <typename T>
+static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs, int64_t ld,
+                                   bool transpose, const Tuning &tn, cudaStream_t st)
+{
+    const int view_upper = row_view_upper(h, transpose);
+    for (int r0 = 0; r0 < nrhs; r0 += 32) {
+        const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
+        int kind = tn.kind;
+        MixTable *mt = nullptr;
+        if (kind == kRowMix || kind < 0) {
+            CAPSP_TRY(ensure_mix(h, group_rows_for(nb), tn.border, view_upper, &mt));
+            if (kind < 0)
+                kind = mt->wo > 0.0 ? kRowMix : kRowWrtFst;
+        }
+        CAPSP_CUDA(launch_fill_pending<T>(x + r0, h->n, nb, ld, h->d_ticket, 1,
+                                          r0 == 0 ? h->d_err : nullptr, st));
+        RowArgs<T> a;
+        a.ptr = h->d_ptr;
+        a.idx = h->d_idx;
+        a.val = (const T *)h->d_val;
+        a.inv_diag = (const T *)h->d_inv;
+        a.b = b + r0;
+        a.x = x + r0;
+        a.ld = ld;
+        a.n = h->n;
+        a.nrhs = nb;
+        a.upper = view_upper;
+        a.table = kind == kRowMix ? mt->d : nullptr;
+        a.table_len = kind == kRowMix ? mt->len : 0;
+        a.ticket = h->d_ticket;
+        a.err = h->d_err;
+        a.wait = h->wait;
+        a.stuck_row = h->stuck_row;
+        const bool prof = h->profiling && r0 == 0;
+        if (prof)
+            CAPSP_CUDA(cudaEventRecord(h->ev_k0, st));
+        CAPSP_CUDA(launch_row_solve<T>(a, kind, tn.R, tn.block, tn.bps, h->num_sms, st));
+        if (prof)
+            CAPSP_CUDA(cudaEventRecord(h->ev_k1, st));
+    }
+    return CAPSP_OK;
+}
+
+template <typename T>
+static capsp_status_t enqueue_cols(capsp_handle_t h, const T *b, T *x, int nrhs, int64_t ld,
+                                   int backward, const T *xf, T *grad, const Tuning &tn,
+                                   cudaStream_t st)
+{
+    CAPSP_TRY(ensure_column_scratch(h, nrhs));
+    for (int r0 = 0; r0 < nrhs; r0 += 32) {
+        const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
+        CAPSP_CUDA(cudaMemsetAsync(h->d_arrived, 0, sizeof(int) * (size_t)h->n, st));
+        CAPSP_CUDA(cudaMemsetAsync(h->d_left, 0, h->vbytes * (size_t)h->n * (size_t)nb, st));
+        CAPSP_CUDA(cudaMemsetAsync(h->d_ticket, 0, sizeof(unsigned), st));
+        if (r0 == 0)
+            CAPSP_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int) * 4, st));
+        ColArgs<T> a;
+        a.ptr = h->d_ptr;
+        a.idx = h->d_idx;
+        a.val = (const T *)h->d_val;
+        a.inv_diag = (const T *)h->d_inv;
+        a.indeg = h->d_indeg;
+        a.arrived = h->d_arrived;
+        a.left_sum = (T *)h->d_left;
+        a.lsld = nb;
+        a.b = b + r0;
+        a.x = x + r0;
+        a.ld = ld;
+        a.n = h->n;
+        a.nrhs = nb;
+        a.backward = backward;
+        a.xf = xf ? xf + r0 : nullptr;
+        a.grad_val = grad;
+        a.grad_accumulate = r0 > 0;
+        a.ticket = h->d_ticket;
+        a.err = h->d_err;
+        a.wait = h->wait;
+        a.stuck_row = h->stuck_row;
+        const bool prof = h->profiling && r0 == 0;
+        if (prof)
+            CAPSP_CUDA(cudaEventRecord(h->ev_k0, st));
+        CAPSP_CUDA(launch_col_solve<T>(a, tn.block, tn.bps, h->num_sms, st));
+        if (prof)
+            CAPSP_CUDA(cudaEventRecord(h->ev_k1, st));
+    }
+    return CAPSP_OK;
+}
+
+enum Op { kOpSolve, kOpTranspose, kOpTransposeGrad };
+
+template <typename T>
+static capsp_status_t enqueue_op(capsp_handle_t h, Op op, const T *in, T *out, const T *xf, T *grad,
+                                 int nrhs, int64_t ld, const Tuning &tn, cudaStream_t st)
+{
+    const bool transpose = op != kOpSolve;
+    const bool row_path = (h->format == CAPSP_FMT_CSR) != transpose;
+    if (op == kOpTransposeGrad && h->format != CAPSP_FMT_CSR)
+        return fail(CAPSP_ERR_UNSUPPORTED, "the fused transpose+gradient sweep needs a CSR handle");
+    if (row_path)
+        return enqueue_rows<T>(h, in, out, nrhs, ld, transpose, tn, st);
+    // column path: CSC solve (forward for lower) or CSR transpose (backward for lower)
+    const int backward = transpose ? (h->uplo == CAPSP_LOWER) : (h->uplo == CAPSP_UPPER);
+    return enqueue_cols<T>(h, in, out, nrhs, ld, backward, xf, grad, tn, st);
+}
+
+static capsp_status_t check_vec_args(capsp_handle_t h, const void *a, const void *b, int nrhs, int64_t ld)
+{
+    if (!h)
+        return fail(CAPSP_ERR_INVALID, "handle is NULL");
+    if (!a || !b)
+        return fail(CAPSP_ERR_INVALID, "vector pointers must be non-NULL");
+    if (nrhs < 1 || ld < nrhs)
+        return fail(CAPSP_ERR_INVALID, "need nrhs >= 1 and ld >= nrhs (got %d, %lld)", nrhs, (long long)ld);
+    if (a == b)
+        return fail(CAPSP_ERR_INVALID, "input and output must not alias");
+    return CAPSP_OK;
+}
+
+static capsp_status_t dispatch(capsp_handle_t h, Op op, const void *in, void *out, const void *xf,
+                               void *grad, int nrhs, int64_t ld, cudaStream_t st)
+{
+    const Tuning tn = current_tuning(h, nrhs);
+    if (h->dtype == CAPSP_R_64F)
+        return enqueue_op<double>(h, op, (const double *)in, (double *)out, (const double *)xf,
+                                  (double *)grad, nrhs, ld, tn, st);
+    return enqueue_op<float>(h, op, (const float *)in, (float *)out, (const float *)xf, (float *)grad,
+                             nrhs, ld, tn, st);
+}
+
+extern "C" capsp_status_t capsp_solve(capsp_handle_t h, const void *b, void *x, int nrhs, int64_t ld,
+                                      void *stream)
+{
+    CAPSP_TRY(check_vec_args(h, b, x, nrhs, ld));
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    return dispatch(h, kOpSolve, b, x, nullptr, nullptr, nrhs, ld, (cudaStream_t)stream);
+}
+
+extern "C" capsp_status_t capsp_solve_transpose(capsp_handle_t h, const void *gv, void *y, int nrhs,
+                                                int64_t ld, void *stream)
+{
+    CAPSP_TRY(check_vec_args(h, gv, y, nrhs, ld));
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    return dispatch(h, kOpTranspose, gv, y, nullptr, nullptr, nrhs, ld, (cudaStream_t)stream);
+}
+
+extern "C" capsp_status_t capsp_solve_transpose_grad(capsp_handle_t h, const void *gv, const void *x,
+                                                     void *y, void *grad_val, int nrhs, int64_t ld,
+                                                     void *stream)
+{
+    CAPSP_TRY(check_vec_args(h, gv, y, nrhs, ld));
+    if (!x || !grad_val)
+        return fail(CAPSP_ERR_INVALID, "x and grad_val must be non-NULL");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    return dispatch(h, kOpTransposeGrad, gv, y, x, grad_val, nrhs, ld, (cudaStream_t)stream);
+}
+
+extern "C" capsp_status_t capsp_grad_val(capsp_handle_t h, const void *y, const void *x, void *grad_val,
+                                         int nrhs, int64_t ld, void *stream)
+{
+    CAPSP_TRY(check_vec_args(h, y, x, nrhs, ld));
+    if (!grad_val)
+        return fail(CAPSP_ERR_INVALID, "grad_val must be non-NULL");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    // CSR: grad[k] = -y[row] x[col]; CSC stores (col j, row idx[k]): swap roles
+    const bool csr = h->format == CAPSP_FMT_CSR;
+    for (int r0 = 0; r0 < nrhs; r0 += 32) {
+        const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
+        if (h->dtype == CAPSP_R_64F) {
+            const double *yy = (const double *)y + r0, *xx = (const double *)x + r0;
+            CAPSP_CUDA(launch_grad_val<double>(h->d_ptr, h->d_idx, csr ? yy : xx, csr ? xx : yy,
+                                               (double *)grad_val, h->n, nb, ld, r0 > 0, st));
+        } else {
+            const float *yy = (const float *)y + r0, *xx = (const float *)x + r0;
+            CAPSP_CUDA(launch_grad_val<float>(h->d_ptr, h->d_idx, csr ? yy : xx, csr ? xx : yy,
+                                              (float *)grad_val, h->n, nb, ld, r0 > 0, st));
+        }
+    }
+    return CAPSP_OK;
+}
+
+// allocate every lazily-built product a solve with nrhs right-hand sides needs
+static capsp_status_t prepare(capsp_handle_t h, int nrhs, bool transpose)
+{
+    const bool row_path = (h->format == CAPSP_FMT_CSR) != transpose;
+    if (row_path) {
+        const Tuning tn = current_tuning(h, nrhs);
+        if (tn.kind == kRowMix || tn.kind < 0) {
+            MixTable *mt = nullptr;
+            for (int r0 = 0; r0 < nrhs; r0 += 32) {
+                const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
+                CAPSP_TRY(ensure_mix(h, group_rows_for(nb), tn.border, row_view_upper(h, transpose), &mt));
+            }
+        }
+        return CAPSP_OK;
+    }
+    return ensure_column_scratch(h, nrhs);
+}
+
+extern "C" capsp_status_t capsp_reserve(capsp_handle_t h, int max_nrhs)
+{
+    if (!h || max_nrhs < 1)
+        return fail(CAPSP_ERR_INVALID, "need a handle and max_nrhs >= 1");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    CAPSP_TRY(prepare(h, max_nrhs, false));
+    CAPSP_TRY(prepare(h, max_nrhs, true));
+    return CAPSP_OK;
+}
+
+extern "C" capsp_status_t capsp_status_sync(capsp_handle_t h, void *stream)
+{
+    if (!h)
+        return fail(CAPSP_ERR_INVALID, "handle is NULL");
+    DeviceGuard g(h->device);
+    CAPSP_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    int err[4] = {0, 0, 0, 0};
+    CAPSP_CUDA(cudaMemcpy(err, h->d_err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err[kErrStatus] == kStatusTimeout)
+        return fail(CAPSP_ERR_TIMEOUT,
+                    "dependency wait ran out of its budget (row/column %d waiting on %d); the "
+                    "affected results are NaN",
+                    err[kErrRow], err[kErrWaitedOn]);
+    if (err[kErrStatus] != 0)
+        return fail(CAPSP_ERR_CUDA, "device reported status %d", err[kErrStatus]);
+    return CAPSP_OK;
+}
+
+extern "C" capsp_status_t capsp_solve_host(capsp_handle_t h, const void *b_host, void *x_host, int nrhs)
+{
+    CAPSP_TRY(check_vec_args(h, b_host, x_host, nrhs, nrhs));
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    const size_t bytes = h->vbytes * (size_t)h->n * (size_t)nrhs;
+    if (h->stage_bytes < 2 * bytes) {
+        cudaFree(h->d_stage);
+        h->d_stage = nullptr;
+        h->stage_bytes = 0;
+        CAPSP_CUDA(cudaMalloc(&h->d_stage, 2 * bytes));
+        h->stage_bytes = 2 * bytes;
+    }
+    if (!h->stage_stream)
+        CAPSP_CUDA(cudaStreamCreateWithFlags(&h->stage_stream, cudaStreamNonBlocking));
+    char *db = (char *)h->d_stage, *dx = db + bytes;
+    cudaStream_t st = h->stage_stream;
+    CAPSP_CUDA(cudaMemcpyAsync(db, b_host, bytes, cudaMemcpyHostToDevice, st));
+    CAPSP_TRY(dispatch(h, kOpSolve, db, dx, nullptr, nullptr, nrhs, nrhs, st));
+    CAPSP_CUDA(cudaMemcpyAsync(x_host, dx, bytes, cudaMemcpyDeviceToHost, st));
+    return capsp_status_sync(h, st);
+}
+
+// ---------------------------------------------------------------------------
+// autotuner
+// ---------------------------------------------------------------------------
+
+extern "C" capsp_status_t capsp_autotune(capsp_handle_t h, const void *b, void *x, int nrhs, int64_t ld,
+                                         void *stream, float *best_ms)
+{
+    CAPSP_TRY(check_vec_args(h, b, x, nrhs, ld));
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<Tuning> cands;
+    const bool row_path = h->format == CAPSP_FMT_CSR;
+    const int blocks[3] = {128, 256, 512};
+    if (row_path) {
+        const int rs[3] = {1, 2, 4};
+        const bool allow_thread = h->alg == CAPSP_ALG_AUTO || h->alg == CAPSP_ALG_WRTFST;
+        const bool allow_mix = h->alg == CAPSP_ALG_AUTO || h->alg == CAPSP_ALG_MIX;
+        if (allow_thread)
+            for (int bl : blocks)
+                for (int r : rs)
+                    cands.push_back({kRowWrtFst, r, bl, 0, h->border});
+        if (h->alg == CAPSP_ALG_TWOPART)
+            for (int bl : blocks)
+                for (int r : rs)
+                    cands.push_back({kRowTwoPart, r, bl, 0, h->border});
+        if (allow_mix) {
+            const int borders[4] = {4, 8, 16, 32};
+            for (int bl : blocks)
+                for (int bo : borders)
+                    cands.push_back({kRowMix, 1, bl, 0, bo});
+        }
+    } else {
+        for (int bl : blocks)
+            cands.push_back({kRowWrtFst, 1, bl, 0, h->border});
+    }
+    cudaEvent_t e0, e1;
+    CAPSP_CUDA(cudaEventCreate(&e0));
+    CAPSP_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    Tuning best_t = cands[0];
+    capsp_status_t st_all = CAPSP_OK;
+    for (const Tuning &tn : cands) {
+        // build tables / scratch outside the timed region
+        if (row_path && tn.kind == kRowMix) {
+            MixTable *mt = nullptr;
+            for (int r0 = 0; r0 < nrhs && st_all == CAPSP_OK; r0 += 32) {
+                const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
+                st_all = ensure_mix(h, group_rows_for(nb), tn.border, row_view_upper(h, false), &mt);
+            }
+        }
+        if (st_all != CAPSP_OK)
+            break;
+        float tot = 0.f;
+        for (int rep = 0; rep < 4 && st_all == CAPSP_OK; ++rep) {
+            cudaEventRecord(e0, st);
+            if (h->dtype == CAPSP_R_64F)
+                st_all = enqueue_op<double>(h, kOpSolve, (const double *)b, (double *)x, nullptr, nullptr,
+                                            nrhs, ld, tn, st);
+            else
+                st_all = enqueue_op<float>(h, kOpSolve, (const float *)b, (float *)x, nullptr, nullptr,
+                                           nrhs, ld, tn, st);
+            cudaEventRecord(e1, st);
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                st_all = fail(CAPSP_ERR_CUDA, "autotune launch failed");
+                break;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0)
+                tot += ms;
+        }
+        if (st_all != CAPSP_OK)
+            break;
+        const float avg = tot / 3.f;
+        if (avg < best) {
+            best = avg;
+            best_t = tn;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CAPSP_TRY(st_all);
+    CAPSP_TRY(capsp_status_sync(h, stream));
+    h->tuned[nrhs] = best_t;
+    if (best_ms)
+        *best_ms = best;
+    return CAPSP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// CUDA graph replay
+// ---------------------------------------------------------------------------
+
+extern "C" capsp_status_t capsp_graph_solve(capsp_handle_t h, const void *b, void *x, int nrhs, int64_t ld,
+                                            void *stream)
+{
+    CAPSP_TRY(check_vec_args(h, b, x, nrhs, ld));
+    if (!stream)
+        return fail(CAPSP_ERR_INVALID,
+                    "graph replay needs an explicit (non-default) stream to capture on");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    const Tuning tn = current_tuning(h, nrhs);
+    const GraphKey key(b, x, nrhs, ld, stream, tn.kind * 1000003 + tn.R * 10007 + tn.block * 101 + tn.border);
+    auto it = h->graphs.find(key);
+    if (it == h->graphs.end()) {
+        CAPSP_TRY(prepare(h, nrhs, false));
+        CAPSP_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        capsp_status_t s = dispatch(h, kOpSolve, b, x, nullptr, nullptr, nrhs, ld, st);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(st, &graph);
+        if (s != CAPSP_OK) {
+            if (graph)
+                cudaGraphDestroy(graph);
+            return s;
+        }
+        if (e != cudaSuccess)
+            return fail(CAPSP_ERR_CUDA, "stream capture failed: %s", cudaGetErrorString(e));
+        cudaGraphExec_t exec = nullptr;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess)
+            return fail(CAPSP_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+        it = h->graphs.emplace(key, exec).first;
+    }
+    CAPSP_CUDA(cudaGraphLaunch(it->second, st));
+    return CAPSP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// kernel timing
+// ---------------------------------------------------------------------------
+
+extern "C" capsp_status_t capsp_set_profiling(capsp_handle_t h, int enable)
+{
+    if (!h)
+        return fail(CAPSP_ERR_INVALID, "handle is NULL");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    if (enable && !h->ev_k0) {
+        CAPSP_CUDA(cudaEventCreate(&h->ev_k0));
+        CAPSP_CUDA(cudaEventCreate(&h->ev_k1));
+    }
+    h->profiling = enable != 0;
+    return CAPSP_OK;
+}
+
+extern "C" capsp_status_t capsp_last_kernel_ms(capsp_handle_t h, float *ms)
+{
+    if (!h || !ms)
+        return fail(CAPSP_ERR_INVALID, "handle and ms must be non-NULL");
+    if (!h->ev_k0)
+        return fail(CAPSP_ERR_INVALID, "profiling was never enabled on this handle");
+    DeviceGuard g(h->device);
+    CAPSP_CUDA(cudaEventSynchronize(h->ev_k1));
+    CAPSP_CUDA(cudaEventElapsedTime(ms, h->ev_k0, h->ev_k1));
+    return CAPSP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// info
+// ---------------------------------------------------------------------------
+
+extern "C" capsp_status_t capsp_get_info(capsp_handle_t h, capsp_info_t *info)
+{
+    if (!h || !info)
+        return fail(CAPSP_ERR_INVALID, "handle and info must be non-NULL");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    memset(info, 0, sizeof(*info));
+    info->n = h->n;
+    info->nnz = h->nnz;
+    info->dtype = h->dtype;
+    info->format = h->format;
+    info->uplo = h->uplo;
+    info->analyse_ms = h->analyse_ms;
+    info->num_sms = h->num_sms;
+    Tuning tn = current_tuning(h, 1);
+    info->rows_per_thread = tn.R;
+    info->block_threads = tn.block;
+    info->blocks_per_sm = tn.bps;
+    if (h->format == CAPSP_FMT_CSC) {
+        info->algorithm = CAPSP_ALG_SYNCFREE_CSC;
+    } else {
+        int alg = h->alg;
+        auto mit = h->mix.find(32);
+        if (mit != h->mix.end() && mit->second.d) {
+            info->mix_len = mit->second.len;
+            info->warp_occupy = mit->second.wo;
+            info->element_occupy = mit->second.eo;
+            if (alg == CAPSP_ALG_AUTO)
+                alg = mit->second.wo > 0.0 ? CAPSP_ALG_MIX : CAPSP_ALG_WRTFST;
+        }
+        info->algorithm = alg;
+    }
+    return CAPSP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// per-hop latency probe
+// ---------------------------------------------------------------------------
+
+extern "C" capsp_status_t capsp_hop_latency(int n, int stride, int dtype, float *ns_per_hop)
+{
+    if (n < 2 || stride < 1 || stride >= n || !ns_per_hop)
+        return fail(CAPSP_ERR_INVALID, "need n >= 2, 1 <= stride < n and an output pointer");
+    if (dtype != CAPSP_R_64F && dtype != CAPSP_R_32F)
+        return fail(CAPSP_ERR_INVALID, "unknown dtype %d", dtype);
+    // row i: x_i = (1 + 0.5 x_{i-stride}) / 1  ->  chain of n/stride hops
+    std::vector<int> ptr((size_t)n + 1), idx;
+    std::vector<double> v64;
+    idx.reserve((size_t)2 * n);
+    v64.reserve((size_t)2 * n);
+    ptr[0] = 0;
+    for (int i = 0; i < n; ++i) {
+        if (i >= stride) {
+            idx.push_back(i - stride);
+            v64.push_back(-0.5);
+        }
+        idx.push_back(i);
+        v64.push_back(1.0);
+        ptr[i + 1] = (int)idx.size();
+    }
+    const int nnz = (int)idx.size();
+    std::vector<float> v32(v64.begin(), v64.end());
+    const void *val = dtype == CAPSP_R_64F ? (const void *)v64.data() : (const void *)v32.data();
+    capsp_handle_t h = nullptr;
+    CAPSP_TRY(capsp_analyse(n, nnz, ptr.data(), idx.data(), val, dtype, CAPSP_FMT_CSR, CAPSP_LOWER, 0, &h));
+    const size_t vb = dtype == CAPSP_R_64F ? 8 : 4;
+    void *d_b = nullptr, *d_x = nullptr;
+    std::vector<double> ones64((size_t)n, 1.0);
+    std::vector<float> ones32((size_t)n, 1.0f);
+    cudaError_t e = cudaMalloc(&d_b, vb * n);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&d_x, vb * n);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(d_b, dtype == CAPSP_R_64F ? (const void *)ones64.data() : (const void *)ones32.data(),
+                       vb * n, cudaMemcpyHostToDevice);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float best = 1e30f;
+    capsp_status_t st = CAPSP_OK;
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&e0);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&e1);
+    for (int rep = 0; rep < 5 && e == cudaSuccess && st == CAPSP_OK; ++rep) {
+        cudaEventRecord(e0, 0);
+        st = capsp_solve(h, d_b, d_x, 1, 1, 0);
+        cudaEventRecord(e1, 0);
+        e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best)
+            best = ms;
+    }
+    if (st == CAPSP_OK && e == cudaSuccess)
+        st = capsp_status_sync(h, 0);
+    if (e0)
+        cudaEventDestroy(e0);
+    if (e1)
+        cudaEventDestroy(e1);
+    cudaFree(d_b);
+    cudaFree(d_x);
+    capsp_destroy(h);
+    if (e != cudaSuccess)
+        return fail(CAPSP_ERR_CUDA, "hop latency probe failed: %s", cudaGetErrorString(e));
+    CAPSP_TRY(st);
+    const double hops = (double)(n - 1) / stride;
+    *ns_per_hop = (float)(best * 1e6 / hops);
+    return CAPSP_OK;
+}

@@ -1,0 +1,126 @@
+// Device-side building blocks shared by the sync-free solve kernels (sm_103a).
+//
+// Readiness protocol ("value as flag").  The reference keeps a separate
+// int flag per row and publishes x[i] with  x store -> __threadfence() ->
+// flag store  (CUDA/ourWrtFst/spts_syncfree_cuda_csr_wrt.h:49-52); a consumer
+// needs one L2 round trip for the flag and another for x.  Here every x
+// element is first filled with a signalling-NaN bit pattern (kPending) that
+// no floating-point operation can produce (IEEE arithmetic quietens NaNs), and
+// the producer publishes the value itself with one relaxed gpu-scope store.
+// A consumer polls the x element with relaxed gpu-scope loads (served by L2,
+// never by a stale L1 line) until it differs from kPending; the value it reads
+// is the dependency.  Aligned 32/64-bit accesses are single-copy atomic, so a
+// reader sees either kPending or the complete value.  One store, no fence,
+// one round trip per hop.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace capsp {
+
+constexpr unsigned kFullMask = 0xffffffffu;
+
+// device error word layout (int[4]): status, row that gave up, index it waited on
+enum { kErrStatus = 0, kErrRow = 1, kErrWaitedOn = 2 };
+constexpr int kStatusTimeout = 2;  // == CAPSP_ERR_TIMEOUT
+
+template <typename T>
+struct VBits;
+
+template <>
+struct VBits<double> {
+    typedef unsigned long long U;
+    static constexpr U kPending = 0x7FF4000000000BADull;  // signalling NaN (quiet bit clear)
+    static constexpr U kQNaN = 0x7FF8000000000000ull;
+    __device__ __forceinline__ static U to(double v) { return (U)__double_as_longlong(v); }
+    __device__ __forceinline__ static double from(U u) { return __longlong_as_double((long long)u); }
+};
+
+template <>
+struct VBits<float> {
+    typedef unsigned int U;
+    static constexpr U kPending = 0x7FA00BADu;  // signalling NaN (quiet bit clear)
+    static constexpr U kQNaN = 0x7FC00000u;
+    __device__ __forceinline__ static U to(float v) { return __float_as_uint(v); }
+    __device__ __forceinline__ static float from(U u) { return __uint_as_float(u); }
+};
+
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned int ld_relaxed(const unsigned int *p)
+{
+    unsigned int v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ int ld_acquire(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_relaxed(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ void st_relaxed(unsigned int *p, unsigned int v)
+{
+    asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long global_timer_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Budget of one dependency wait.
+struct WaitCfg {
+    unsigned long long timeout_ns;  // wall-clock budget of a single wait
+    unsigned max_iters;             // iteration cap (backstop for the timer)
+    unsigned sleep_max_ns;          // ceiling of the exponential __nanosleep backoff
+};
+
+// Bounded spin with exponential backoff.  next() returns true when the wait
+// must be abandoned: the budget ran out (this thread records TIMEOUT in the
+// error word) or another thread already recorded an error.
+struct Spin {
+    unsigned it;
+    unsigned long long t0;
+    __device__ __forceinline__ Spin() : it(0), t0(0) {}
+    __device__ __forceinline__ bool next(int *err, const WaitCfg &w, int row, int waited_on)
+    {
+        ++it;
+        if (it > 4u && w.sleep_max_ns) {
+            unsigned s = 32u << (it - 5u < 6u ? it - 5u : 6u);
+            __nanosleep(s < w.sleep_max_ns ? s : w.sleep_max_ns);
+        }
+        if ((it & 15u) == 0u) {
+            if (ld_relaxed(reinterpret_cast<const unsigned *>(err)) != 0u)
+                return true;
+            const unsigned long long now = global_timer_ns();
+            if (t0 == 0ull) {
+                t0 = now;
+            } else if (now - t0 > w.timeout_ns || it > w.max_iters) {
+                if (atomicCAS(err + kErrStatus, 0, kStatusTimeout) == 0) {
+                    err[kErrRow] = row;
+                    err[kErrWaitedOn] = waited_on;
+                }
+                return true;
+            }
+        }
+        return false;
+    }
+};
+
+}  // namespace capsp

@@ -1,0 +1,105 @@
+// Internal interface between the C-ABI layer (capsp_api.cu, capsp_compat.cu)
+// and the kernel translation units.  Not installed; no C-ABI types here.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "capsp_device.cuh"
+
+namespace capsp {
+
+// Arguments of the row-driven solve (thread / two-phase / mix kernels).
+// Logical ("solve order") row p maps to physical row i = p for lower and
+// i = n-1-p for upper matrices; the diagonal is the last entry of a lower
+// row and the first entry of an upper row.
+template <typename T>
+struct RowArgs {
+    const int *ptr;
+    const int *idx;
+    const T *val;
+    const T *inv_diag;
+    const T *b;
+    T *x;
+    long long ld;  // element (i, r) at i*ld + r
+    int n;
+    int nrhs;      // right-hand sides handled by this launch (<= 32)
+    int upper;
+    const int *table;  // mix virtual-warp table in solve order (MIX only)
+    int table_len;
+    unsigned *ticket;
+    int *err;
+    WaitCfg wait;
+    int stuck_row;  // debug: this row never publishes (-1: none)
+};
+
+// Arguments of the column-driven solve (SyncFree CSC kernel, and the
+// transpose solve that walks CSR rows as columns of the transpose).
+template <typename T>
+struct ColArgs {
+    const int *ptr;
+    const int *idx;
+    const T *val;
+    const T *inv_diag;
+    const int *indeg;  // entries targeting each row, diagonal included
+    int *arrived;      // zeroed before the launch
+    T *left_sum;       // zeroed before the launch, element (i, r) at i*lsld + r
+    long long lsld;
+    const T *b;
+    T *x;
+    long long ld;
+    int n;
+    int nrhs;  // <= 32
+    int backward;  // columns visited n-1..0, diagonal last in each column
+    const T *xf;   // forward solution for the fused grad_val (nullptr: no grad)
+    T *grad_val;
+    int grad_accumulate;  // add into grad_val instead of overwriting
+    unsigned *ticket;
+    int *err;
+    WaitCfg wait;
+    int stuck_row;
+};
+
+enum RowKernelKind { kRowWrtFst = 1, kRowTwoPart = 2, kRowMix = 3 };
+
+// lanes per row for a launch with nrhs right-hand sides (next power of two, <= 32)
+inline int lanes_for_rhs(int nrhs)
+{
+    int g = 1;
+    while (g < nrhs && g < 32)
+        g <<= 1;
+    return g;
+}
+
+template <typename T>
+cudaError_t launch_row_solve(const RowArgs<T> &a, int kind, int rows_per_thread, int block,
+                             int blocks_per_sm, int num_sms, cudaStream_t st);
+
+template <typename T>
+cudaError_t launch_col_solve(const ColArgs<T> &a, int block, int blocks_per_sm, int num_sms,
+                             cudaStream_t st);
+
+// x[i*ld + r] = pending pattern for i < n, r < nrhs; ticket[0..nticket) = 0; err[0..3] = 0
+template <typename T>
+cudaError_t launch_fill_pending(T *x, int n, int nrhs, long long ld, unsigned *ticket, int nticket,
+                                int *err, cudaStream_t st);
+
+// inv[i] = 1/val[diag(i)]; records the first row with a zero or non-finite diagonal in *bad
+template <typename T>
+cudaError_t launch_inv_diag(const int *ptr, const T *val, T *inv, int n, int diag_last, int *bad,
+                            cudaStream_t st);
+
+template <typename T>
+cudaError_t launch_grad_val(const int *rowptr, const int *colidx, const T *y, const T *x,
+                            T *grad_val, int n, int nrhs, long long ld, int accumulate,
+                            cudaStream_t st);
+
+// structure check on device arrays; *bad = first bad row (must be preset to INT_MAX)
+cudaError_t launch_validate(const int *ptr, const int *idx, int n, int nnz, int diag_last,
+                            int *bad, cudaStream_t st);
+
+// out[idx[k]] += 1 (out must be zeroed)
+cudaError_t launch_histogram(const int *idx, int nnz, int *out, cudaStream_t st);
+
+}  // namespace capsp

@@ -1,0 +1,300 @@
+/*
+ * Host preprocessing for the sync-free triangular solve: structure checks,
+ * level statistics, the mix selector table, transposition, the in-degree
+ * analyser, b = L*ones and a Matrix Market reader.  Written against the
+ * contracts of the reference's host helpers (CUDA/ourWrtFst/read_mtx.h,
+ * CUDA/ourWrtFst/tranpose.h, CUDA/mix/tranpose.h) -- see each function.
+ */
+#include "capsp.h"
+
+#include <ctype.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ */
+/* small helpers                                                        */
+/* ------------------------------------------------------------------ */
+
+/* Stable sort of (col, value) pairs of one row by col; values are opaque
+ * blobs of vbytes bytes.  Insertion sort for short rows, merge sort above. */
+static void sort_row_pairs_generic(int *col, unsigned char *val, size_t vbytes, int cnt)
+{
+    if (cnt < 2)
+        return;
+    if (cnt <= 64) {
+        unsigned char tmp[16];
+        for (int t = 1; t < cnt; ++t) {
+            int c = col[t];
+            memcpy(tmp, val + (size_t)t * vbytes, vbytes);
+            int u = t - 1;
+            while (u >= 0 && col[u] > c) {
+                col[u + 1] = col[u];
+                memcpy(val + (size_t)(u + 1) * vbytes, val + (size_t)u * vbytes, vbytes);
+                --u;
+            }
+            col[u + 1] = c;
+            memcpy(val + (size_t)(u + 1) * vbytes, tmp, vbytes);
+        }
+        return;
+    }
+    int *c2 = (int *)malloc(sizeof(int) * (size_t)cnt);
+    unsigned char *v2 = (unsigned char *)malloc(vbytes * (size_t)cnt);
+    if (!c2 || !v2) { /* fall back to the quadratic path */
+        free(c2);
+        free(v2);
+        for (int t = 1; t < cnt; ++t) {
+            unsigned char tmp[16];
+            int c = col[t];
+            memcpy(tmp, val + (size_t)t * vbytes, vbytes);
+            int u = t - 1;
+            while (u >= 0 && col[u] > c) {
+                col[u + 1] = col[u];
+                memcpy(val + (size_t)(u + 1) * vbytes, val + (size_t)u * vbytes, vbytes);
+                --u;
+            }
+            col[u + 1] = c;
+            memcpy(val + (size_t)(u + 1) * vbytes, tmp, vbytes);
+        }
+        return;
+    }
+    for (int width = 1; width < cnt; width *= 2) {
+        for (int lo = 0; lo < cnt; lo += 2 * width) {
+            int mid = lo + width < cnt ? lo + width : cnt;
+            int hi = lo + 2 * width < cnt ? lo + 2 * width : cnt;
+            int a = lo, b = mid, w = lo;
+            while (a < mid || b < hi) {
+                int take_a = (b >= hi) || (a < mid && col[a] <= col[b]);
+                int src = take_a ? a++ : b++;
+                c2[w] = col[src];
+                memcpy(v2 + (size_t)w * vbytes, val + (size_t)src * vbytes, vbytes);
+                ++w;
+            }
+        }
+        memcpy(col, c2, sizeof(int) * (size_t)cnt);
+        memcpy(val, v2, vbytes * (size_t)cnt);
+    }
+    free(c2);
+    free(v2);
+}
+
+void capsp_exclusive_scan(int *input, int length)
+{
+    if (length <= 1) {
+        if (length == 1)
+            input[0] = 0;
+        return;
+    }
+    int running = 0;
+    for (int i = 0; i < length; ++i) {
+        int v = input[i];
+        input[i] = running;
+        running += v;
+    }
+}
+
+/* Selector over `group_rows`-row groups in solve order.  The table lists the
+ * first solve-order row of every virtual warp plus a final end entry; its
+ * length is returned.  Mirrors matrix_warp4 (CUDA/mix/tranpose.h:1423-1483). */
+static int mix_table_impl(int n, const int *rowptr, int upper, int group_rows, int border,
+                          int nnz, int *table, double *wo, double *eo)
+{
+    double row_warp = 0.0, elem_warp = 0.0;
+    int k = 1, row = 0;
+    table[0] = 0;
+    for (int p0 = 0; p0 < n; p0 += group_rows) {
+        int p1 = p0 + group_rows < n ? p0 + group_rows : n;
+        int elems = upper ? rowptr[n - p0] - rowptr[n - p1] : rowptr[p1] - rowptr[p0];
+        double avg = (double)elems / (double)(p1 - p0);
+        if (avg >= (double)border) {
+            elem_warp += (double)elems;
+            row_warp += (double)(p1 - p0);
+            for (int t = p0; t < p1; ++t)
+                table[k++] = ++row;
+        } else {
+            row += p1 - p0;
+            table[k++] = row;
+        }
+    }
+    *wo = n > 0 ? row_warp / n : 0.0;
+    *eo = nnz > 0 ? elem_warp / nnz : 0.0;
+    return k;
+}
+
+int capsp_mix_table(int n, const int *rowptr, int upper, int group_rows, int border, int *table,
+                    double *warp_occupy, double *element_occupy)
+{
+    double wo = 0.0, eo = 0.0;
+    if (n < 0 || group_rows < 1 || !rowptr || !table)
+        return 0;
+    int len = mix_table_impl(n, rowptr, upper, group_rows, border, rowptr[n] - rowptr[0], table,
+                             &wo, &eo);
+    if (warp_occupy)
+        *warp_occupy = wo;
+    if (element_occupy)
+        *element_occupy = eo;
+    return len;
+}
+
+/* Level recurrence of matrix_layer (CUDA/ourWrtFst/tranpose.h:95-117): every
+ * row's level is one more than the deepest level among its stored columns,
+ * where columns not yet visited (the diagonal itself) count as level 0. */
+int capsp_row_levels(int n, const int *rowptr, const int *colidx, int *level, int *level_count)
+{
+    memset(level, 0, sizeof(int) * (size_t)(n > 0 ? n : 1));
+    if (level_count)
+        memset(level_count, 0, sizeof(int) * ((size_t)n + 1));
+    int deepest = 0;
+    for (int row = 0; row < n; ++row) {
+        int lv = 0;
+        for (int j = rowptr[row]; j < rowptr[row + 1]; ++j) {
+            int c = level[colidx[j]] + 1;
+            if (c > lv)
+                lv = c;
+        }
+        level[row] = lv;
+        if (level_count)
+            level_count[lv]++;
+        if (lv > deepest)
+            deepest = lv;
+    }
+    return deepest;
+}
+
+void capsp_indegree(int n, int nnz, const int *idx, int *indeg)
+{
+    memset(indeg, 0, sizeof(int) * (size_t)(n > 0 ? n : 1));
+    for (int k = 0; k < nnz; ++k)
+        indeg[idx[k]]++;
+}
+
+int capsp_validate(int n, int nnz, const int *ptr, const int *idx, int format, int uplo, char *msg,
+                   int msg_len)
+{
+    char local[8];
+    if (!msg || msg_len <= 0) {
+        msg = local;
+        msg_len = (int)sizeof(local);
+    }
+    msg[0] = 0;
+    if (n < 1 || nnz < n) {
+        snprintf(msg, (size_t)msg_len, "need n >= 1 and nnz >= n (got n=%d nnz=%d)", n, nnz);
+        return -1;
+    }
+    if (ptr[0] != 0 || ptr[n] != nnz) {
+        snprintf(msg, (size_t)msg_len, "ptr[0]=%d ptr[n]=%d, expected 0 and nnz=%d", ptr[0], ptr[n],
+                 nnz);
+        return -1;
+    }
+    const int diag_last = (format == CAPSP_FMT_CSR) == (uplo == CAPSP_LOWER);
+    for (int i = 0; i < n; ++i) {
+        const int s = ptr[i], e = ptr[i + 1];
+        if (e <= s || e > nnz) {
+            snprintf(msg, (size_t)msg_len, "row/column %d is empty or its pointer is out of order", i);
+            return -(i + 2);
+        }
+        const int dpos = diag_last ? e - 1 : s;
+        if (idx[dpos] != i) {
+            snprintf(msg, (size_t)msg_len, "row/column %d: diagonal missing from its %s position", i,
+                     diag_last ? "last" : "first");
+            return -(i + 2);
+        }
+        for (int j = s; j < e; ++j) {
+            if (j == dpos)
+                continue;
+            const int c = idx[j];
+            const int ok = diag_last ? (c >= 0 && c < i) : (c > i && c < n);
+            if (!ok) {
+                snprintf(msg, (size_t)msg_len,
+                         "row/column %d: index %d is not on the triangular side of the diagonal", i, c);
+                return -(i + 2);
+            }
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Matrix Market parsing (coordinate format)                           */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    int m, n, nnz;
+    int field;     /* 0 real, 1 integer, 2 pattern */
+    int symmetric; /* symmetric or hermitian: mirror off-diagonal entries */
+} mm_header_t;
+
+static void lower_str(char *s)
+{
+    for (; *s; ++s)
+        *s = (char)tolower((unsigned char)*s);
+}
+
+static int mm_read_header(FILE *f, mm_header_t *hd)
+{
+    char line[1100], t0[64], t1[64], t2[64], t3[64], t4[64];
+    if (!fgets(line, sizeof(line), f))
+        return -2;
+    if (sscanf(line, "%63s %63s %63s %63s %63s", t0, t1, t2, t3, t4) != 5)
+        return -2;
+    lower_str(t0);
+    lower_str(t1);
+    lower_str(t2);
+    lower_str(t3);
+    lower_str(t4);
+    if (strcmp(t0, "%%matrixmarket") != 0 || strcmp(t1, "matrix") != 0)
+        return -2;
+    if (strcmp(t2, "coordinate") != 0)
+        return -3;
+    if (strcmp(t3, "complex") == 0)
+        return -3;
+    if (strcmp(t3, "real") == 0 || strcmp(t3, "double") == 0)
+        hd->field = 0;
+    else if (strcmp(t3, "integer") == 0)
+        hd->field = 1;
+    else if (strcmp(t3, "pattern") == 0)
+        hd->field = 2;
+    else
+        return -3;
+    hd->symmetric = (strcmp(t4, "symmetric") == 0 || strcmp(t4, "hermitian") == 0);
+    do {
+        if (!fgets(line, sizeof(line), f))
+            return -4;
+    } while (line[0] == '%' || line[0] == '\n' || line[0] == '\r');
+    if (sscanf(line, "%d %d %d", &hd->m, &hd->n, &hd->nnz) != 3 || hd->m < 0 || hd->n < 0 ||
+        hd->nnz < 0)
+        return -4;
+    return 0;
+}
+
+static int mm_read_entry(FILE *f, const mm_header_t *hd, int *a, int *b, double *v)
+{
+    if (hd->field == 2) {
+        *v = 1.0;
+        return fscanf(f, "%d %d", a, b) == 2 ? 0 : -1;
+    }
+    if (hd->field == 1) {
+        long iv;
+        if (fscanf(f, "%d %d %ld", a, b, &iv) != 3)
+            return -1;
+        *v = (double)iv;
+        return 0;
+    }
+    return fscanf(f, "%d %d %lg", a, b, v) == 3 ? 0 : -1;
+}
+
+/* ------------------------------------------------------------------ */
+/* value-type generic functions                                        */
+/* ------------------------------------------------------------------ */
+
+#define VT double
+#define SFX(x) x##_f64
+#include "preprocess_impl.h"
+#undef VT
+#undef SFX
+
+#define VT float
+#define SFX(x) x##_f32
+#include "preprocess_impl.h"
+#undef VT
+#undef SFX

@@ -1,0 +1,216 @@
+// Column-driven sync-free triangular solve for sm_103a: one warp per column,
+// the SyncFree design of sptrsv_syncfree_cuda_executor_update
+// (CUDA/SyncFree_csc/spts_syncfree_cuda2.h:24-86) and of the serial executor
+// (openCL/SynFree_csc/sptrsv_syncfree_serialref.h:25-108).
+//
+// A column j waits until every other entry of its row has been scattered
+// (arrived[j] == indeg[j] - 1), computes x_j = (b_j - left_sum_j) * (1/diag),
+// then scatters x_j * L_rj into left_sum[r] for the column's off-diagonal
+// rows and counts them in arrived[r].  FORWARD visits columns 0..n-1 with the
+// diagonal first in each column; BACKWARD visits n-1..0 with the diagonal
+// last.  BACKWARD on the CSR arrays of a lower-triangular L is the transpose
+// solve L^T y = g without building L^T: row i of L is column i of L^T.
+//
+// Differences from the reference kernel:
+//   * counters count up from zero (no in-degree restore copy per solve);
+//   * every waiting lane performs its own acquire load, then reads left_sum
+//     through L2; producers issue all their fp64 reductions, one fence, a
+//     warp barrier, then the counter increments;
+//   * multi-RHS: G = next_pow2(nrhs) lanes per entry, one right-hand side
+//     each; 32/G entries per warp pass;
+//   * optional fused gradient: while column j's values y_j are in registers
+//     the warp also writes grad_val[k] = -sum_r y[j,r] * xf[idx[k], r] for
+//     every stored entry k of the column (diagonal included);
+//   * bounded waits with the same Spin budget as the row kernels.
+#pragma once
+
+#include "capsp_internal.h"
+
+namespace capsp {
+
+template <typename T, int G>
+__global__ void __launch_bounds__(512) col_solve_kernel(const ColArgs<T> a)
+{
+    typedef VBits<T> VB;
+    typedef typename VB::U U;
+    constexpr int EPW = 32 / G;
+    const int lane = threadIdx.x & 31;
+    const int es = lane / G, g = lane % G;
+    const bool active = g < a.nrhs;
+    for (;;) {
+        unsigned tk = 0, stop = 0;
+        if (lane == 0) {
+            tk = atomicAdd(a.ticket, 1u);
+            stop = ld_relaxed(reinterpret_cast<const unsigned *>(a.err));
+        }
+        tk = __shfl_sync(kFullMask, tk, 0);
+        stop = __shfl_sync(kFullMask, stop, 0);
+        if (stop || tk >= (unsigned)a.n)
+            break;
+        const int j = a.backward ? a.n - 1 - (int)tk : (int)tk;
+        const int s0 = __ldg(a.ptr + j), e0 = __ldg(a.ptr + j + 1);
+        const int s = a.backward ? s0 : s0 + 1;
+        const int e = a.backward ? e0 - 1 : e0;
+        const int need = __ldg(a.indeg + j) - 1;
+        const T dinv = __ldg(a.inv_diag + j);
+        bool aborted = false;
+        T xj = T(0);
+        if (es == 0 && active) {
+            const size_t xo = (size_t)j * (size_t)a.ld + g;
+            const T bj = __ldg(a.b + xo);
+            Spin sp;
+            while (ld_acquire(a.arrived + j) != need) {
+                if (sp.next(a.err, a.wait, j, j)) {
+                    aborted = true;
+                    break;
+                }
+            }
+            const T ls = VB::from(ld_relaxed(reinterpret_cast<const U *>(a.left_sum) +
+                                             (size_t)j * (size_t)a.lsld + g));
+            xj = aborted ? VB::from(VB::kQNaN) : (bj - ls) * dinv;
+            a.x[xo] = xj;
+        }
+        xj = __shfl_sync(kFullMask, xj, g);
+        if (j != a.stuck_row) {
+            for (int k = s + es; k < e; k += EPW) {
+                const int r = __ldg(a.idx + k);
+                const T v = __ldg(a.val + k);
+                if (active)
+                    atomicAdd(a.left_sum + (size_t)r * (size_t)a.lsld + g, xj * v);
+            }
+            __threadfence();
+            __syncwarp();
+            if (g == 0) {
+                for (int k = s + es; k < e; k += EPW)
+                    atomicAdd(a.arrived + __ldg(a.idx + k), 1);
+            }
+        }
+        if (a.grad_val != nullptr) {
+            for (int kb = s0; kb < e0; kb += EPW) {
+                const int k = kb + es;
+                T prod = T(0);
+                if (k < e0 && active)
+                    prod = xj * __ldg(a.xf + (size_t)__ldg(a.idx + k) * (size_t)a.ld + g);
+#pragma unroll
+                for (int off = G / 2; off >= 1; off >>= 1)
+                    prod += __shfl_xor_sync(kFullMask, prod, off);
+                if (k < e0 && g == 0)
+                    a.grad_val[k] = a.grad_accumulate ? a.grad_val[k] - prod : -prod;
+            }
+        }
+    }
+}
+
+template <typename T, int G>
+static cudaError_t launch_col_impl(const ColArgs<T> &a, int block, int bps, int num_sms,
+                                   cudaStream_t st)
+{
+    auto kern = col_solve_kernel<T, G>;
+    int occ = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, 0);
+    if (e != cudaSuccess)
+        return e;
+    if (occ < 1)
+        occ = 1;
+    const int per_sm = (bps > 0 && bps < occ) ? bps : occ;
+    long long grid = (long long)per_sm * num_sms;
+    const long long need = ((long long)a.n + block / 32 - 1) / (block / 32);
+    if (grid > need)
+        grid = need;
+    if (grid < 1)
+        grid = 1;
+    kern<<<(unsigned)grid, block, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_col_solve(const ColArgs<T> &a, int block, int blocks_per_sm, int num_sms,
+                             cudaStream_t st)
+{
+    switch (lanes_for_rhs(a.nrhs)) {
+    case 1: return launch_col_impl<T, 1>(a, block, blocks_per_sm, num_sms, st);
+    case 2: return launch_col_impl<T, 2>(a, block, blocks_per_sm, num_sms, st);
+    case 4: return launch_col_impl<T, 4>(a, block, blocks_per_sm, num_sms, st);
+    case 8: return launch_col_impl<T, 8>(a, block, blocks_per_sm, num_sms, st);
+    case 16: return launch_col_impl<T, 16>(a, block, blocks_per_sm, num_sms, st);
+    default: return launch_col_impl<T, 32>(a, block, blocks_per_sm, num_sms, st);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// analysis helpers and the standalone gradient
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void inv_diag_kernel(const int *__restrict__ ptr, const T *__restrict__ val,
+                                T *__restrict__ inv, int n, int diag_last, int *bad)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const int pos = diag_last ? ptr[i + 1] - 1 : ptr[i];
+    const T d = val[pos];
+    if (!(d != T(0)) || !isfinite(d))
+        atomicMin(bad, i);
+    inv[i] = T(1) / d;
+}
+
+template <typename T>
+cudaError_t launch_inv_diag(const int *ptr, const T *val, T *inv, int n, int diag_last, int *bad,
+                            cudaStream_t st)
+{
+    inv_diag_kernel<T><<<(n + 255) / 256, 256, 0, st>>>(ptr, val, inv, n, diag_last, bad);
+    return cudaGetLastError();
+}
+
+// warp per row: 32/G entries x G right-hand sides per pass
+template <typename T, int G>
+__global__ void grad_val_kernel(const int *__restrict__ rowptr, const int *__restrict__ colidx,
+                                const T *__restrict__ y, const T *__restrict__ x,
+                                T *__restrict__ grad, int n, int nrhs, long long ld,
+                                int accumulate)
+{
+    constexpr int EPW = 32 / G;
+    const int lane = threadIdx.x & 31;
+    const int es = lane / G, g = lane % G;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long i = warp; i < n; i += nwarps) {
+        const int s = rowptr[i], e = rowptr[i + 1];
+        const T yi = g < nrhs ? y[(size_t)i * ld + g] : T(0);
+        for (int kb = s; kb < e; kb += EPW) {
+            const int k = kb + es;
+            T prod = T(0);
+            if (k < e && g < nrhs)
+                prod = yi * x[(size_t)colidx[k] * ld + g];
+#pragma unroll
+            for (int off = G / 2; off >= 1; off >>= 1)
+                prod += __shfl_xor_sync(kFullMask, prod, off);
+            if (k < e && g == 0)
+                grad[k] = accumulate ? grad[k] - prod : -prod;
+        }
+    }
+}
+
+template <typename T>
+cudaError_t launch_grad_val(const int *rowptr, const int *colidx, const T *y, const T *x,
+                            T *grad_val, int n, int nrhs, long long ld, int accumulate,
+                            cudaStream_t st)
+{
+    long long blocks = ((long long)n * 32 + 255) / 256;
+    if (blocks > 65536)
+        blocks = 65536;
+    if (blocks < 1)
+        blocks = 1;
+    switch (lanes_for_rhs(nrhs)) {
+    case 1: grad_val_kernel<T, 1><<<(unsigned)blocks, 256, 0, st>>>(rowptr, colidx, y, x, grad_val, n, nrhs, ld, accumulate); break;
+    case 2: grad_val_kernel<T, 2><<<(unsigned)blocks, 256, 0, st>>>(rowptr, colidx, y, x, grad_val, n, nrhs, ld, accumulate); break;
+    case 4: grad_val_kernel<T, 4><<<(unsigned)blocks, 256, 0, st>>>(rowptr, colidx, y, x, grad_val, n, nrhs, ld, accumulate); break;
+    case 8: grad_val_kernel<T, 8><<<(unsigned)blocks, 256, 0, st>>>(rowptr, colidx, y, x, grad_val, n, nrhs, ld, accumulate); break;
+    case 16: grad_val_kernel<T, 16><<<(unsigned)blocks, 256, 0, st>>>(rowptr, colidx, y, x, grad_val, n, nrhs, ld, accumulate); break;
+    default: grad_val_kernel<T, 32><<<(unsigned)blocks, 256, 0, st>>>(rowptr, colidx, y, x, grad_val, n, nrhs, ld, accumulate); break;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace capsp

@@ -1,0 +1,276 @@
+"""GPU parity of the sync-free solves against the oracle (the reference's serial
+executor restated in C, pinned bit-for-bit by tests/test_oracle.py).
+
+Tolerances (relative infinity-norm error against the FP64 oracle):
+  FP64: 1e-12          FP32: 1e-5 against the FP32 oracle
+All calls go through the C-ABI (capellinisptrsv_gb300 binds it with ctypes).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import capellinisptrsv_gb300 as cs
+import oracle
+from conftest import rel_inf_err
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+TOL64, TOL32 = 1e-12, 1e-5
+DEV = "cuda:0"
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(DEV)
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def solver_for(m, dtype=np.float64, on_device=True, **kw):
+    val = m.val.astype(dtype)
+    if on_device:
+        return cs.TriangularSolver(dev(m.rowptr), dev(m.colidx), dev(val), **kw)
+    return cs.TriangularSolver(m.rowptr, m.colidx, val, **kw)
+
+
+@pytest.fixture(scope="module")
+def plain20k():
+    return cs.generate("plain_20k", seed=0)
+
+
+@pytest.mark.parametrize("alg", ["wrtfst", "twopart", "mix", "auto"])
+@pytest.mark.parametrize("on_device", [True, False])
+def test_plain_20k_fp64(plain20k, alg, on_device):
+    m = plain20k
+    _, b = cs.get_x_b(m.n, m.n, m.rowptr, m.colidx, m.val)
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
+    s = solver_for(m, on_device=on_device, algorithm=alg)
+    x = host(s.solve(dev(b)))
+    s.status()
+    assert rel_inf_err(x, xo) <= TOL64
+    assert np.max(np.abs(x - 1.0)) <= 0.01  # the reference's own self-check (x_ref = ones)
+
+
+def test_plain_20k_fp32_and_its_fp64_error(plain20k):
+    m = plain20k
+    v32 = m.val.astype(np.float32)
+    _, b32 = cs.get_x_b(m.n, m.n, m.rowptr, m.colidx, v32)
+    x32o = oracle.solve_csr_lower(m.rowptr, m.colidx, v32, b32)
+    _, b64 = cs.get_x_b(m.n, m.n, m.rowptr, m.colidx, m.val)
+    x64o = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b64)
+    s = solver_for(m, np.float32)
+    x = host(s.solve(dev(b32)))
+    assert rel_inf_err(x, x32o) <= TOL32
+    err64 = rel_inf_err(x, x64o)   # stated, not bounded by the FP32 tolerance alone
+    print(f"FP32 result vs FP64 oracle: {err64:.3e}")
+    assert err64 < 1e-4
+
+
+@pytest.mark.parametrize("rows_per_thread", [1, 2, 4])
+@pytest.mark.parametrize("block", [64, 256, 512])
+def test_launch_shapes(plain20k, rows_per_thread, block):
+    m = plain20k
+    b = cs.normal(m.n, seed=1)
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
+    s = solver_for(m)
+    s.set_tuning(rows_per_thread, block, 0)
+    x = host(s.solve(dev(b)))
+    assert rel_inf_err(x, xo) <= TOL64
+
+
+def test_deterministic_and_schedules_agree(plain20k):
+    """Sums are taken in storage order whatever the arrival order: repeated solves
+    and the write-first / two-phase schedules give identical bits."""
+    m = plain20k
+    b = dev(cs.normal(m.n, seed=2))
+    s = solver_for(m, algorithm="wrtfst")
+    x1, x2 = host(s.solve(b)), host(s.solve(b))
+    s.set_algorithm("twopart")
+    x3 = host(s.solve(b))
+    assert np.array_equal(x1.view(np.uint64), x2.view(np.uint64))
+    assert np.array_equal(x1.view(np.uint64), x3.view(np.uint64))
+
+
+EDGE = ["single", "diagonal_only", "bidiagonal_chain", "stride64_chain", "dense_band_40", "row_512",
+        "ragged_33", "full_lower_64"]
+
+
+@pytest.mark.parametrize("name", EDGE)
+@pytest.mark.parametrize("alg", ["wrtfst", "twopart", "mix"])
+def test_edge_cases_against_golden(golden, name, alg):
+    rp, ci, v = (golden[f"edge_{name}_{k}"] for k in ("rowptr", "colidx", "val"))
+    n = len(rp) - 1
+    b1 = np.random.default_rng(11).standard_normal(n)
+    b4 = np.random.default_rng(12).standard_normal((n, 4))
+    s = cs.TriangularSolver(dev(rp), dev(ci), dev(v), algorithm=alg)
+    s.set_mix_border(4)
+    assert rel_inf_err(host(s.solve(dev(b1))), golden[f"edge_{name}_x1"]) <= TOL64
+    assert rel_inf_err(host(s.solve(dev(b4))), golden[f"edge_{name}_x4"]) <= TOL64
+    assert rel_inf_err(host(s.solve_transpose(dev(b1))), golden[f"edge_{name}_y1"]) <= TOL64
+    assert rel_inf_err(host(s.solve_transpose(dev(b4))), golden[f"edge_{name}_y4"]) <= TOL64
+    s.status()
+
+
+@pytest.mark.parametrize("nrhs", [1, 2, 3, 4, 8, 16, 32, 40])
+def test_multi_rhs_forward_adjoint_grad(nrhs):
+    m = cs.generate(n=30_000, kmin=1, kmax=9, band=3000, seed=nrhs)
+    b = np.random.default_rng(nrhs).standard_normal((m.n, nrhs))
+    g = np.random.default_rng(nrhs + 100).standard_normal((m.n, nrhs))
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
+    yo = oracle.solve_csr_transpose(m.rowptr, m.colidx, m.val, g)
+    go = oracle.grad_val(m.rowptr, m.colidx, yo, xo)
+    s = solver_for(m)
+    x = s.solve(dev(b))
+    y, gv = s.solve_transpose_grad(dev(g), x)
+    y2 = s.solve_transpose(dev(g))
+    gv2 = s.grad_val(y2, x)
+    s.status()
+    assert rel_inf_err(host(x), xo) <= TOL64
+    assert rel_inf_err(host(y), yo) <= TOL64
+    assert rel_inf_err(host(y2), yo) <= TOL64
+    assert rel_inf_err(host(gv), go) <= TOL64
+    assert rel_inf_err(host(gv2), go) <= TOL64
+
+
+def test_strided_rhs_layout():
+    """ld > nrhs: a column slice of a wider buffer."""
+    m = cs.generate(n=5000, kmin=1, kmax=5, band=500, seed=8)
+    wide = np.random.default_rng(0).standard_normal((m.n, 7))
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, wide[:, 2:5])
+    bt = dev(wide)
+    xt = torch.full_like(bt, 123.0)
+    s = solver_for(m)
+    s.solve(bt[:, 2:5], xt[:, 2:5])
+    out = host(xt)
+    assert rel_inf_err(out[:, 2:5], xo) <= TOL64
+    assert np.all(out[:, :2] == 123.0) and np.all(out[:, 5:] == 123.0)
+
+
+def test_wide_4m_full_size_fp64_and_fp32():
+    """The 4M-row workload at full size against the oracle (it finishes in well under a second)."""
+    m = cs.generate("wide_4m", seed=0)
+    _, b = cs.get_x_b(m.n, m.n, m.rowptr, m.colidx, m.val)
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
+    s = solver_for(m)
+    x = host(s.solve(dev(b)))
+    s.status()
+    assert rel_inf_err(x, xo) <= TOL64
+    v32 = m.val.astype(np.float32)
+    _, b32 = cs.get_x_b(m.n, m.n, m.rowptr, m.colidx, v32)
+    x32o = oracle.solve_csr_lower(m.rowptr, m.colidx, v32, b32)
+    s32 = solver_for(m, np.float32)
+    x32 = host(s32.solve(dev(b32)))
+    assert rel_inf_err(x32, x32o) <= TOL32
+    print(f"wide_4m FP32 vs FP64 oracle: {rel_inf_err(x32, xo):.3e}")
+
+
+def test_zipf_mix_path():
+    m = cs.generate("zipf_1m", seed=0, n=200_000)
+    b = cs.normal(m.n, seed=3)
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
+    s = solver_for(m, algorithm="mix")
+    x = host(s.solve(dev(b)))
+    s.status()
+    info = s.info()
+    assert info["warp_occupy"] > 0.0  # heavy groups went warp-per-row
+    assert rel_inf_err(x, xo) <= TOL64
+
+
+def test_upper_csr_and_csc_paths():
+    """Upper-triangular CSR (backward substitution) and the CSC warp-per-column
+    kernel, forward and transposed, against the oracle on the same matrix."""
+    m = cs.generate(n=20_000, kmin=1, kmax=6, band=900, seed=5)
+    cp, ri, cv = cs.matrix_transposition(m.n, m.n, m.nnz, m.rowptr, m.colidx, m.val)
+    b = cs.normal(m.n, seed=6)
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)   # L x = b
+    yo = oracle.solve_csr_transpose(m.rowptr, m.colidx, m.val, b)  # L^T y = b
+    # CSC of L == CSR of U = L^T (diagonal first in each row)
+    up = cs.TriangularSolver(dev(cp), dev(ri), dev(cv), uplo="upper")
+    assert rel_inf_err(host(up.solve(dev(b))), yo) <= TOL64
+    assert rel_inf_err(host(up.solve_transpose(dev(b))), xo) <= TOL64
+    csc = cs.TriangularSolver(dev(cp), dev(ri), dev(cv), fmt="csc")
+    assert rel_inf_err(host(csc.solve(dev(b))), xo) <= TOL64
+    assert rel_inf_err(host(csc.solve_transpose(dev(b))), yo) <= TOL64
+    b4 = np.random.default_rng(4).standard_normal((m.n, 4))
+    assert rel_inf_err(host(csc.solve(dev(b4))),
+                       oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b4)) <= TOL64
+    up.status()
+    csc.status()
+
+
+def test_set_values_refreshes(plain20k):
+    m = plain20k
+    s = solver_for(m)
+    b = cs.normal(m.n, seed=7)
+    v2 = m.val * 1.5
+    s.set_values(dev(v2))
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, v2, b)
+    assert rel_inf_err(host(s.solve(dev(b))), xo) <= TOL64
+
+
+def test_solve_host_buffers(plain20k):
+    m = plain20k
+    s = solver_for(m, on_device=False)
+    b = cs.normal((m.n * 2), seed=8).reshape(m.n, 2)
+    x = s.solve_host(b)
+    assert rel_inf_err(x, oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)) <= TOL64
+
+
+def test_graph_replay_and_autotune(plain20k):
+    m = plain20k
+    s = solver_for(m)
+    b = dev(cs.normal(m.n, seed=9))
+    x = torch.empty_like(b)
+    st = torch.cuda.Stream()
+    ms = s.autotune(b, x, stream=st)
+    assert ms > 0
+    with torch.cuda.stream(st):
+        for _ in range(3):
+            s.graph_solve(b, x, st)
+    st.synchronize()
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, host(b))
+    assert rel_inf_err(host(x), xo) <= TOL64
+
+
+def test_invalid_matrices_are_rejected():
+    rp = np.array([0, 1, 3], np.int32)
+    bad_ci = np.array([0, 1, 0], np.int32)  # row 1: diagonal not last
+    v = np.ones(3)
+    with pytest.raises(cs.CapspError) as e:
+        cs.TriangularSolver(rp, bad_ci, v)
+    assert e.value.status == 1
+    with pytest.raises(cs.CapspError):
+        cs.TriangularSolver(dev(rp), dev(bad_ci), dev(v))
+    with pytest.raises(cs.CapspError):  # zero diagonal
+        cs.TriangularSolver(rp, np.array([0, 0, 1], np.int32), np.array([1.0, 1.0, 0.0]))
+
+
+def test_timeout_is_reported_and_context_survives(plain20k):
+    """A row that never publishes (debug hook): its dependants' waits run out
+    after 20 ms, the solve reports TIMEOUT, and the next solve is clean."""
+    m = plain20k
+    s = solver_for(m)
+    b = dev(cs.normal(m.n, seed=10))
+    s.debug_stuck_row(5000, timeout_s=0.02)
+    x = s.solve(b)
+    with pytest.raises(cs.CapspError) as e:
+        s.status()
+    assert e.value.status == 2
+    xh = host(x)
+    assert np.isnan(xh).any()
+    s.debug_stuck_row(-1, timeout_s=10.0)
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, host(b))
+    assert rel_inf_err(host(s.solve(b)), xo) <= TOL64
+    s.status()
+
+
+def test_hop_latency_probe_runs():
+    lat_warp = cs.hop_latency(n=20_000, stride=1)
+    lat_l2 = cs.hop_latency(n=20_000, stride=256)
+    print(f"hop latency: in-warp {lat_warp:.0f} ns, cross-warp {lat_l2:.0f} ns")
+    assert lat_warp > 0 and lat_l2 > 0

@@ -1,0 +1,214 @@
+"""CPU tests of libcapsp's host side: the library loads and exports every
+declared symbol, the generators and host preprocessing match the reference's
+contracts (golden vectors from the reference itself), structure checks."""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import capellinisptrsv_gb300 as cs
+from capellinisptrsv_gb300 import _native as N
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_functions():
+    """Functions declared by the library headers (capsp_compat.h only holds inline
+    wrappers over these and is checked by compiling against it)."""
+    names = []
+    for hdr in sorted((ROOT / "include").glob("*.h")):
+        if hdr.name == "capsp_compat.h":
+            continue
+        text = re.sub(r"/\*.*?\*/", "", hdr.read_text(), flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b([a-z_][a-z0-9_]*)\s*\(", text, flags=re.M):
+            name = m.group(1)
+            if name not in ("if", "defined", "sizeof", "return"):
+                names.append(name)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    names = declared_functions()
+    assert len(names) > 40
+    missing = [n for n in names if not hasattr(N.lib, n)]
+    assert not missing, missing
+    # and the Python binding declares a signature for each of them
+    assert not [n for n in names if n not in N.EXPORTED]
+
+
+COMPAT_C = r"""
+#define CAPSP_COMPAT_HOST
+#include "capsp_compat.h"
+int use(const int *rp, const int *ci, const VT *v, int n, int nnz) {
+    double t, g, bw, pre, wo, eo; int layer; double par;
+    int *lrp, *lci; VT *lv; int nnzL; VT *x, *b;
+    matrix_layer(n, n, nnz, rp, ci, v, &layer, &par);
+    get_x_b(n, n, rp, ci, v, &x, &b);
+    change2tran(n, nnz, (int *)rp, (int *)ci, (VT *)v, &nnzL, &lrp, &lci, &lv);
+    sptrsv_syncfree_cuda(rp, ci, v, n, n, nnz, x, b, x, &pre, &t, &g, &bw);
+    return spts_syncfree_cuda_csr_wrt(rp, ci, v, n, n, nnz, &t, &g, &bw) +
+           spts_syncfree_cuda_csr(rp, ci, v, n, n, nnz, &t, &g, &bw) + (int)(pre + wo + eo);
+}
+"""
+
+
+@pytest.mark.parametrize("lang,vt", [("c", "double"), ("c", "float"), ("c++", "double"), ("c++", "float")])
+def test_compat_header_compiles_and_links(tmp_path, lang, vt):
+    """Reference-style code (unsuffixed names, VALUE_TYPE chosen by the caller)
+    compiles against capsp_compat.h and links against libcapsp.so."""
+    import subprocess
+    src = tmp_path / ("use.c" if lang == "c" else "use.cpp")
+    src.write_text(COMPAT_C.replace("VT", vt))
+    out = tmp_path / "libuse.so"
+    cc = ["gcc", "-std=c11"] if lang == "c" else ["g++", "-std=c++17"]
+    lib = ROOT / "capellinisptrsv_gb300" / "_build"
+    r = subprocess.run([*cc, "-shared", "-fPIC", "-Werror", "-Wall", "-Wno-unused-variable",
+                        "-Wno-uninitialized", "-Wno-maybe-uninitialized", "-I", str(ROOT / "include"),
+                        str(src), "-L", str(lib), "-lcapsp", "-o", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_generator_is_deterministic_and_follows_the_rules():
+    a = cs.generate(n=7000, kmin=1, kmax=7, band=600, seed=3)
+    b = cs.generate(n=7000, kmin=1, kmax=7, band=600, seed=3)
+    assert a.digest() == b.digest()
+    assert cs.generate(n=7000, kmin=1, kmax=7, band=600, seed=4).digest() != a.digest()
+    rp, ci, v = a.rowptr, a.colidx, a.val
+    for i in range(a.n):
+        cols, vals = ci[rp[i]:rp[i + 1]], v[rp[i]:rp[i + 1]]
+        k = len(cols) - 1
+        assert cols[-1] == i
+        assert k <= 7 and (k >= 1 or i == 0)
+        assert np.all(np.diff(cols) > 0)
+        assert np.all(cols[:-1] >= max(0, i - 600))
+        assert np.all(np.abs(vals[:-1]) <= 1.0)
+        assert vals[-1] == 1.0 + np.sum(np.abs(vals[:-1]))
+
+
+def test_zipf_generator_near_far_rule():
+    m = cs.generate(n=20_000, kind=N.GEN_ZIPF_NEAR_FAR, zipf_s=1.8, zipf_cap=512, near_window=32, seed=1)
+    ks = np.diff(m.rowptr) - 1
+    assert ks.max() <= 512 and ks[100:].min() >= 1
+    i = 10_000
+    cols = m.colidx[m.rowptr[i]:m.rowptr[i + 1] - 1]
+    k = len(cols)
+    assert np.sum(cols >= i - 32) >= (k + 1) // 2
+
+
+def test_normal_generator_moments():
+    z = cs.normal(200_000, seed=5)
+    assert abs(z.mean()) < 0.01 and abs(z.std() - 1.0) < 0.01
+    assert np.array_equal(z, cs.normal(200_000, seed=5))
+
+
+def test_change2tran_matches_reference(golden):
+    rp, ci, va = golden["pre_A_rowptr"].copy(), golden["pre_A_colidx"].copy(), golden["pre_A_val"].copy()
+    nnzL, lrp, lci, lv = cs.change2tran(len(rp) - 1, rp, ci, va)
+    assert nnzL == len(golden["pre_L_colidx"])
+    assert np.array_equal(lrp, golden["pre_L_rowptr"])
+    assert np.array_equal(lci, golden["pre_L_colidx"])
+    assert np.array_equal(lv, golden["pre_L_val"])
+
+
+def test_layer_transposition_warp4_match_reference(golden):
+    lrp, lci, lv = golden["pre_L_rowptr"], golden["pre_L_colidx"], golden["pre_L_val"]
+    n = len(lrp) - 1
+    lay, par = cs.matrix_layer(n, n, len(lci), lrp, lci, lv)
+    assert lay == int(golden["pre_L_layer"][0]) and par == float(golden["pre_L_parallelism"][0])
+    cp, ri, cv = cs.matrix_transposition(n, n, len(lci), lrp, lci, lv)
+    assert np.array_equal(cp, golden["pre_L_csc_colptr"])
+    assert np.array_equal(ri, golden["pre_L_csc_rowidx"])
+    assert np.array_equal(cv, golden["pre_L_csc_val"])
+    for border in (0, 2, 3, 10):
+        ln, table, wo, eo = cs.matrix_warp4(n, n, len(lci), lrp, lci, lv, border=border)
+        assert np.array_equal(table, golden[f"pre_warp4_{border}_table"])
+        assert [wo, eo] == list(golden[f"pre_warp4_{border}_occ"])
+
+
+def test_workload_stats_match_reference(golden):
+    import hashlib
+    m = cs.generate("plain_20k", seed=0)
+    lay, par = cs.matrix_layer(m.n, m.n, m.nnz, m.rowptr, m.colidx, m.val)
+    assert lay == int(golden["plain_20k_layer"][0])
+    assert par == float(golden["plain_20k_parallelism"][0])
+    ln, table, wo, eo = cs.matrix_warp4(m.n, m.n, m.nnz, m.rowptr, m.colidx, m.val, border=10)
+    assert ln == int(golden["plain_20k_warp4_len"][0])
+    assert [wo, eo] == list(golden["plain_20k_warp4_occ"])
+    assert np.array_equal(np.frombuffer(hashlib.sha256(table.tobytes()).digest(), np.uint8),
+                          golden["plain_20k_warp4_sha"])
+
+
+@pytest.mark.parametrize("name", ["general", "sym_pattern", "integer"])
+def test_read_mtx_matches_reference(golden, tmp_path, name):
+    p = tmp_path / f"{name}.mtx"
+    p.write_bytes(golden[f"mtx_{name}_text"].tobytes())
+    m, n, nnz, rp, ci, v = cs.read_mtx(str(p))
+    assert (m, n, nnz) == tuple(int(golden[f"mtx_{name}_{k}"]) for k in ("m", "n", "nnz"))
+    assert np.array_equal(rp, golden[f"mtx_{name}_rowptr"])
+    assert np.array_equal(ci, golden[f"mtx_{name}_colidx"])
+    assert np.array_equal(v, golden[f"mtx_{name}_val"])
+
+
+def test_read_mtx_rejects_complex_and_missing(tmp_path):
+    p = tmp_path / "c.mtx"
+    p.write_text("%%MatrixMarket matrix coordinate complex general\n1 1 1\n1 1 1 0\n")
+    with pytest.raises(ValueError):
+        cs.read_mtx(str(p))
+    with pytest.raises(ValueError):
+        cs.read_mtx(str(tmp_path / "nope.mtx"))
+
+
+def test_row_levels_histogram():
+    m = cs.generate(n=3000, kmin=1, kmax=3, band=50, seed=2)
+    levels, level, counts = cs.row_levels(m.n, m.rowptr, m.colidx)
+    assert levels == cs.matrix_layer(m.n, m.n, m.nnz, m.rowptr, m.colidx)[0]
+    assert counts[1:].sum() == m.n and counts[0] == 0
+    for i in (0, 17, 2999):
+        deps = m.colidx[m.rowptr[i]:m.rowptr[i + 1] - 1]
+        assert level[i] == 1 + (level[deps].max() if len(deps) else 0)
+
+
+def _validate(rp, ci, fmt=N.FMT_CSR, uplo=N.LOWER):
+    rp, ci = np.asarray(rp, np.int32), np.asarray(ci, np.int32)
+    msg = C.create_string_buffer(256)
+    rc = N.lib.capsp_validate(len(rp) - 1, len(ci), rp.ctypes.data_as(C.c_void_p), ci.ctypes.data_as(C.c_void_p),
+                              fmt, uplo, msg, 256)
+    return rc, msg.value.decode()
+
+
+def test_validation_catches_malformed_structures():
+    assert _validate([0, 1, 3], [0, 0, 1])[0] == 0
+    assert _validate([0, 1, 3], [0, 1, 0])[0] != 0          # diagonal not last
+    assert _validate([0, 1, 2], [0, 0])[0] != 0             # row 1 lacks its diagonal
+    assert _validate([0, 2, 3], [1, 0, 1])[0] != 0          # upper entry in a lower matrix
+    assert _validate([0, 1, 1], [0])[0] != 0                # empty row
+    assert _validate([0, 1, 3], [0, 1, 0], uplo=N.UPPER)[0] != 0
+    assert _validate([0, 2, 3], [0, 1, 1], uplo=N.UPPER)[0] == 0   # CSR upper: diagonal first
+    assert _validate([0, 2, 3], [0, 1, 1], fmt=N.FMT_CSC)[0] == 0  # CSC lower: diagonal first
+    rc, msg = _validate([0, 1, 2], [0, 0])
+    assert "row/column 1" in msg
+
+
+def test_exclusive_scan_and_indegree():
+    a = np.array([3, 0, 2, 5, 1], np.int32)
+    N.lib.capsp_exclusive_scan(a.ctypes.data_as(C.c_void_p), len(a))
+    assert list(a) == [0, 3, 3, 5, 10]
+    idx = np.array([0, 2, 2, 1, 2], np.int32)
+    deg = np.empty(3, np.int32)
+    N.lib.capsp_indegree(3, 5, idx.ctypes.data_as(C.c_void_p), deg.ctypes.data_as(C.c_void_p))
+    assert list(deg) == [1, 1, 3]
+
+
+def test_batched_generator_is_block_diagonal():
+    m = cs.generate_batched(nsys=12, seed=1, nmin=50, nmax=400)
+    so = m.sys_rowoff
+    assert so[0] == 0 and so[-1] == m.n and len(so) == 13
+    sys_of_row = np.searchsorted(so, np.arange(m.n), side="right") - 1
+    rows = np.repeat(np.arange(m.n), np.diff(m.rowptr))
+    assert np.all(m.colidx >= so[sys_of_row[rows]])
+    assert np.all(m.colidx <= rows)
