@@ -20,6 +20,7 @@ R_64F, R_32F = 0, 1
 FMT_CSR, FMT_CSC = 0, 1
 LOWER, UPPER = 0, 1
 ALG_AUTO, ALG_WRTFST, ALG_TWOPART, ALG_MIX, ALG_SYNCFREE_CSC = range(5)
+SCHED_NATURAL, SCHED_LEVEL = 0, 1
 DEVICE_POINTERS, SKIP_VALIDATION = 0x1, 0x2
 GEN_UNIFORM_BAND, GEN_ZIPF_NEAR_FAR = 0, 1
 
@@ -35,7 +36,8 @@ class Info(C.Structure):
                 ("uplo", C.c_int), ("algorithm", C.c_int), ("mix_len", C.c_int),
                 ("warp_occupy", C.c_double), ("element_occupy", C.c_double),
                 ("analyse_ms", C.c_double), ("rows_per_thread", C.c_int),
-                ("block_threads", C.c_int), ("blocks_per_sm", C.c_int), ("num_sms", C.c_int)]
+                ("block_threads", C.c_int), ("blocks_per_sm", C.c_int), ("num_sms", C.c_int),
+                ("schedule", C.c_int), ("levels", C.c_int)]
 
 
 class GenParams(C.Structure):
@@ -66,10 +68,13 @@ _SIGS = {
     "capsp_analyse": (I, [I, I, P, P, P, I, I, I, C.c_uint, C.POINTER(H)]),
     "capsp_batched_create": (I, [I, P, I, I, P, P, P, I, C.c_uint, C.POINTER(H)]),
     "capsp_set_values": (I, [H, P]),
+    "capsp_refresh_values": (I, [H, P, P]),
+    "capsp_set_backoff": (I, [H, C.c_uint]),
     "capsp_destroy": (I, [H]),
     "capsp_get_info": (I, [H, C.POINTER(Info)]),
     "capsp_set_algorithm": (I, [H, I]),
     "capsp_set_mix_border": (I, [H, I]),
+    "capsp_set_schedule": (I, [H, I]),
     "capsp_set_tuning": (I, [H, I, I, I]),
     "capsp_set_timeout": (I, [H, C.c_uint64]),
     "capsp_solve": (I, [H, P, P, I, C.c_int64, P]),
@@ -85,6 +90,7 @@ _SIGS = {
     "capsp_last_kernel_ms": (I, [H, C.POINTER(C.c_float)]),
     "capsp_device_sms": (I, [IP]),
     "capsp_debug_set_stuck_row": (I, [H, I, C.c_uint64]),
+    "capsp_debug_trace": (I, [H, P]),
     "capsp_hop_latency": (I, [I, I, I, C.POINTER(C.c_float)]),
     # reference-compatible drivers
     "spts_syncfree_cuda_csr_wrt_f64": (I, [P, P, P, I, I, I, DP, DP, DP]),
@@ -112,6 +118,8 @@ _SIGS = {
     "matrix_warp4_f32": (None, [I, I, I, P, P, P, I, IP, P, DP, DP]),
     "capsp_mix_table": (I, [I, P, I, I, I, P, DP, DP]),
     "capsp_indegree": (None, [I, I, P, P]),
+    "capsp_level_schedule": (I, [I, P, P, I, P, P, P]),
+    "capsp_level_layout": (I, [I, P, P, I, P, P, P, P, P, P]),
     "capsp_validate": (I, [I, I, P, P, I, I, C.c_char_p, I]),
     "read_mtx_f64": (I, [C.c_char_p, IP, IP, IP, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
     "read_mtx_f32": (I, [C.c_char_p, IP, IP, IP, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),

@@ -17,7 +17,9 @@ __all__ = ["SparseTriangularSolve", "sptrsv", "DifferentiableTriangular"]
 class SparseTriangularSolve(torch.autograd.Function):
     @staticmethod
     def forward(ctx, val: torch.Tensor, b: torch.Tensor, solver: TriangularSolver):
-        solver.bind_values(val.detach())
+        # values may have changed in place (optimiser steps, .data writes):
+        # re-point and recompute 1/diag on the stream, no synchronisation
+        solver.refresh_values(val.detach())
         x = solver.solve(b.detach())
         ctx.solver = solver
         ctx.save_for_backward(val, x)
@@ -27,7 +29,7 @@ class SparseTriangularSolve(torch.autograd.Function):
     def backward(ctx, gx: torch.Tensor):
         val, x = ctx.saved_tensors
         solver: TriangularSolver = ctx.solver
-        solver.bind_values(val.detach())
+        solver.refresh_values(val.detach())
         gx = gx.contiguous()
         need_val, need_b = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
         if need_val:

@@ -116,10 +116,12 @@ struct capsp_handle_s {
     std::map<int, MixTable> mix;
     int alg = CAPSP_ALG_AUTO;
     int border = 10;
-    Tuning tune = {kRowWrtFst, 2, 256, 0, 10};
+    // measured on GB300 (wide-level solves): one chunk per lane, 8 resident
+    // warps per SM; more resident warps only add pollers
+    Tuning tune = {kRowWrtFst, 1, 256, 1, 10};
     bool tune_explicit = false;
     std::map<int, Tuning> tuned;
-    WaitCfg wait = {10000000000ull, 1u << 30, 1024u};
+    WaitCfg wait = {10000000000ull, 1u << 30, 256u};
     int stuck_row = -1;
     std::map<GraphKey, cudaGraphExec_t> graphs;
     void *d_stage = nullptr;
@@ -128,6 +130,16 @@ struct capsp_handle_s {
     double analyse_ms = 0.0;
     bool profiling = false;
     cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;
+    unsigned long long *trace = nullptr;  // borrowed tracing buffer (2n entries)
+    // level schedule of the row-driven view (positions, capsp_level_layout)
+    int sched = CAPSP_SCHED_LEVEL;
+    bool level_built = false;
+    int levels = 0;
+    int *d_perm = nullptr, *d_lptr = nullptr, *d_lidx = nullptr, *d_lsrc = nullptr, *d_dsrc = nullptr;
+    void *d_lval = nullptr, *d_linv = nullptr;
+    std::vector<int> h_lcum;  // lptr[k] + k: row-count prefix in position space (mix tables)
+    void *d_xp = nullptr;     // position-ordered publication scratch
+    int xp_cap = 0;           // right-hand sides it holds
     int nsys = 0;
     std::vector<int> sys_rowoff;
     std::recursive_mutex mu;
@@ -156,6 +168,14 @@ static void free_handle(capsp_handle_t h)
     cudaFree(h->d_arrived);
     cudaFree(h->d_left);
     cudaFree(h->d_stage);
+    cudaFree(h->d_perm);
+    cudaFree(h->d_lptr);
+    cudaFree(h->d_lidx);
+    cudaFree(h->d_lsrc);
+    cudaFree(h->d_dsrc);
+    cudaFree(h->d_lval);
+    cudaFree(h->d_linv);
+    cudaFree(h->d_xp);
     if (h->stage_stream)
         cudaStreamDestroy(h->stage_stream);
     if (h->ev_k0)
@@ -189,6 +209,81 @@ static capsp_status_t refresh_inv_diag(capsp_handle_t h)
         return fail(CAPSP_ERR_CUDA, "computing 1/diag failed: %s", cudaGetErrorString(e));
     if (bad != INT_MAX)
         return fail(CAPSP_ERR_INVALID, "diagonal entry of row/column %d is zero or not finite", bad);
+    return CAPSP_OK;
+}
+
+// level-schedule values from the handle's current values, on `st`
+static capsp_status_t launch_level_refresh(capsp_handle_t h, int *bad, cudaStream_t st)
+{
+    if (!h->level_built)
+        return CAPSP_OK;
+    if (h->dtype == CAPSP_R_64F)
+        CAPSP_CUDA(launch_level_values<double>(h->d_lptr, h->d_lsrc, h->d_dsrc, h->n, (const double *)h->d_val,
+                                               (double *)h->d_lval, (double *)h->d_linv, bad, st));
+    else
+        CAPSP_CUDA(launch_level_values<float>(h->d_lptr, h->d_lsrc, h->d_dsrc, h->n, (const float *)h->d_val,
+                                              (float *)h->d_lval, (float *)h->d_linv, bad, st));
+    return CAPSP_OK;
+}
+
+// row-driven view of the handle: CSR rows in solve order, or CSC columns read
+// as rows of the transpose
+static int row_view_upper(capsp_handle_t h)
+{
+    return h->format == CAPSP_FMT_CSR ? (h->uplo == CAPSP_UPPER) : (h->uplo == CAPSP_LOWER);
+}
+
+// Build the level schedule of the row-driven view (host work O(nnz) plus one
+// upload); synchronous.
+static capsp_status_t build_level(capsp_handle_t h)
+{
+    if (h->level_built)
+        return CAPSP_OK;
+    const int n = h->n, nnz = h->nnz;
+    const int upper = row_view_upper(h);
+    std::vector<int> idx((size_t)nnz);
+    CAPSP_CUDA(cudaMemcpy(idx.data(), h->d_idx, sizeof(int) * (size_t)nnz, cudaMemcpyDeviceToHost));
+    std::vector<int> order((size_t)n), position((size_t)n), lptr((size_t)n + 1), dsrc((size_t)n);
+    const size_t ndeps = (size_t)nnz - (size_t)n;
+    std::vector<int> lidx(ndeps > 0 ? ndeps : 1), lsrc(ndeps > 0 ? ndeps : 1);
+    const int levels = capsp_level_schedule(n, h->h_ptr.data(), idx.data(), upper, order.data(),
+                                            position.data(), nullptr);
+    if (levels < 0)
+        return fail(CAPSP_ERR_OOM, "host allocation failed while building the level schedule");
+    if (capsp_level_layout(n, h->h_ptr.data(), idx.data(), upper, order.data(), position.data(),
+                           lptr.data(), lidx.data(), lsrc.data(), dsrc.data()) != 0)
+        return fail(CAPSP_ERR_INVALID, "misplaced diagonal while building the level schedule");
+    const size_t vb = h->vbytes;
+    CAPSP_CUDA(cudaMalloc(&h->d_perm, sizeof(int) * (size_t)n));
+    CAPSP_CUDA(cudaMalloc(&h->d_lptr, sizeof(int) * ((size_t)n + 1)));
+    CAPSP_CUDA(cudaMalloc(&h->d_lidx, sizeof(int) * lidx.size()));
+    CAPSP_CUDA(cudaMalloc(&h->d_lsrc, sizeof(int) * lsrc.size()));
+    CAPSP_CUDA(cudaMalloc(&h->d_dsrc, sizeof(int) * (size_t)n));
+    CAPSP_CUDA(cudaMalloc(&h->d_lval, vb * lidx.size()));
+    CAPSP_CUDA(cudaMalloc(&h->d_linv, vb * (size_t)n));
+    CAPSP_CUDA(cudaMemcpy(h->d_perm, order.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
+    CAPSP_CUDA(cudaMemcpy(h->d_lptr, lptr.data(), sizeof(int) * ((size_t)n + 1), cudaMemcpyHostToDevice));
+    CAPSP_CUDA(cudaMemcpy(h->d_lidx, lidx.data(), sizeof(int) * lidx.size(), cudaMemcpyHostToDevice));
+    CAPSP_CUDA(cudaMemcpy(h->d_lsrc, lsrc.data(), sizeof(int) * lsrc.size(), cudaMemcpyHostToDevice));
+    CAPSP_CUDA(cudaMemcpy(h->d_dsrc, dsrc.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
+    h->h_lcum.resize((size_t)n + 1);
+    for (int k = 0; k <= n; ++k)
+        h->h_lcum[k] = lptr[k] + k;
+    h->levels = levels;
+    h->level_built = true;
+    int *d_bad = nullptr;
+    CAPSP_CUDA(cudaMalloc(&d_bad, sizeof(int)));
+    const int big = INT_MAX;
+    int bad = INT_MAX;
+    cudaError_t e = cudaMemcpy(d_bad, &big, sizeof(int), cudaMemcpyHostToDevice);
+    capsp_status_t s = e == cudaSuccess ? launch_level_refresh(h, d_bad, 0) : CAPSP_ERR_CUDA;
+    if (s == CAPSP_OK)
+        e = cudaMemcpy(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d_bad);
+    if (s != CAPSP_OK || e != cudaSuccess)
+        return fail(CAPSP_ERR_CUDA, "level-schedule upload failed");
+    if (bad != INT_MAX)
+        return fail(CAPSP_ERR_INVALID, "zero or non-finite diagonal at schedule position %d", bad);
     return CAPSP_OK;
 }
 
@@ -302,6 +397,8 @@ extern "C" capsp_status_t capsp_analyse(int n, int nnz, const int *ptr, const in
     }
     h->d_err = reinterpret_cast<int *>(h->d_ticket + 64);
     st = refresh_inv_diag(h);
+    if (st == CAPSP_OK && format == CAPSP_FMT_CSR)
+        st = build_level(h);  // the default schedule of the forward solve
     if (st != CAPSP_OK) {
         free_handle(h);
         return st;
@@ -361,7 +458,57 @@ extern "C" capsp_status_t capsp_set_values(capsp_handle_t h, const void *val)
     } else {
         CAPSP_CUDA(cudaMemcpy(h->d_val, val, h->vbytes * (size_t)h->nnz, cudaMemcpyHostToDevice));
     }
-    return refresh_inv_diag(h);
+    CAPSP_TRY(refresh_inv_diag(h));
+    if (h->level_built) {
+        CAPSP_TRY(launch_level_refresh(h, h->d_err + 3, 0));
+        CAPSP_CUDA(cudaDeviceSynchronize());
+    }
+    return CAPSP_OK;
+}
+
+extern "C" capsp_status_t capsp_refresh_values(capsp_handle_t h, const void *val, void *stream)
+{
+    if (!h)
+        return fail(CAPSP_ERR_INVALID, "handle is NULL");
+    if (!(h->flags & CAPSP_DEVICE_POINTERS))
+        return fail(CAPSP_ERR_INVALID,
+                    "capsp_refresh_values needs a CAPSP_DEVICE_POINTERS handle; use capsp_set_values");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    if (val)
+        h->d_val = const_cast<void *>(val);
+    const int dl = diag_last_of(h->format, h->uplo);
+    cudaStream_t st = (cudaStream_t)stream;
+    int *bad = h->d_err + 3;  // sticky diagnostic slot: first row with a bad diagonal
+    if (h->dtype == CAPSP_R_64F)
+        CAPSP_CUDA(launch_inv_diag<double>(h->d_ptr, (const double *)h->d_val, (double *)h->d_inv, h->n, dl, bad, st));
+    else
+        CAPSP_CUDA(launch_inv_diag<float>(h->d_ptr, (const float *)h->d_val, (float *)h->d_inv, h->n, dl, bad, st));
+    return launch_level_refresh(h, bad, st);
+}
+
+extern "C" capsp_status_t capsp_set_schedule(capsp_handle_t h, int schedule)
+{
+    if (!h)
+        return fail(CAPSP_ERR_INVALID, "handle is NULL");
+    if (schedule != CAPSP_SCHED_NATURAL && schedule != CAPSP_SCHED_LEVEL)
+        return fail(CAPSP_ERR_INVALID, "unknown schedule %d", schedule);
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    h->sched = schedule;
+    h->tuned.clear();
+    if (schedule == CAPSP_SCHED_LEVEL)
+        return build_level(h);
+    return CAPSP_OK;
+}
+
+extern "C" capsp_status_t capsp_set_backoff(capsp_handle_t h, unsigned sleep_max_ns)
+{
+    if (!h)
+        return fail(CAPSP_ERR_INVALID, "handle is NULL");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    h->wait.sleep_max_ns = sleep_max_ns;
+    return CAPSP_OK;
 }
 
 extern "C" capsp_status_t capsp_set_algorithm(capsp_handle_t h, int algorithm)
@@ -439,22 +586,20 @@ extern "C" capsp_status_t capsp_debug_set_stuck_row(capsp_handle_t h, int row, u
 // rows per mix group for a launch with nrhs right-hand sides
 static int group_rows_for(int nrhs) { return 32 / lanes_for_rhs(nrhs < 32 ? nrhs : 32); }
 
-// row path view: CSR handles solve their rows; CSC handles read their columns
-// as rows of the transpose
-static int row_view_upper(capsp_handle_t h, bool transpose)
+// Selector table over `group_rows` consecutive schedule positions; its row
+// counts come from the level layout (dependencies + diagonal per position) or,
+// for the natural schedule, from the row pointer of the row-driven view.
+static capsp_status_t ensure_mix(capsp_handle_t h, int group_rows, int border, MixTable **out)
 {
-    return transpose ? (h->uplo == CAPSP_LOWER) : (h->uplo == CAPSP_UPPER);
-}
-
-static capsp_status_t ensure_mix(capsp_handle_t h, int group_rows, int border, bool view_upper,
-                                 MixTable **out)
-{
-    MixTable &mt = h->mix[group_rows];
+    const bool level = h->sched == CAPSP_SCHED_LEVEL;
+    MixTable &mt = h->mix[group_rows * 2 + (level ? 1 : 0)];
     if (mt.d == nullptr || mt.border != border) {
         std::vector<int> table((size_t)h->n + 2);
         double wo = 0.0, eo = 0.0;
-        const int len = capsp_mix_table(h->n, h->h_ptr.data(), view_upper ? 1 : 0, group_rows,
-                                        border, table.data(), &wo, &eo);
+        const int len = level ? capsp_mix_table(h->n, h->h_lcum.data(), 0, group_rows, border, table.data(),
+                                                &wo, &eo)
+                              : capsp_mix_table(h->n, h->h_ptr.data(), row_view_upper(h), group_rows, border,
+                                                table.data(), &wo, &eo);
         if (mt.d == nullptr)
             CAPSP_CUDA(cudaMalloc(&mt.d, sizeof(int) * ((size_t)h->n + 2)));
         CAPSP_CUDA(cudaMemcpy(mt.d, table.data(), sizeof(int) * (size_t)len, cudaMemcpyHostToDevice));
@@ -508,27 +653,59 @@ static Tuning current_tuning(capsp_handle_t h, int nrhs)
 // enqueue paths
 // ---------------------------------------------------------------------------
 
+// position-ordered publication scratch for the level schedule
+static capsp_status_t ensure_xp(capsp_handle_t h, int nrhs)
+{
+    const int want = nrhs < 32 ? nrhs : 32;
+    if (h->xp_cap < want) {
+        cudaFree(h->d_xp);
+        h->d_xp = nullptr;
+        h->xp_cap = 0;
+        CAPSP_CUDA(cudaMalloc(&h->d_xp, h->vbytes * (size_t)h->n * (size_t)want));
+        h->xp_cap = want;
+    }
+    return CAPSP_OK;
+}
+
 template <typename T>
 static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs, int64_t ld,
-                                   bool transpose, const Tuning &tn, cudaStream_t st)
+                                   const Tuning &tn, cudaStream_t st)
 {
-    const int view_upper = row_view_upper(h, transpose);
+    const int view_upper = row_view_upper(h);
+    const bool level = h->sched == CAPSP_SCHED_LEVEL;
+    if (level) {
+        CAPSP_TRY(build_level(h));
+        CAPSP_TRY(ensure_xp(h, nrhs));
+    }
     for (int r0 = 0; r0 < nrhs; r0 += 32) {
         const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
         int kind = tn.kind;
         MixTable *mt = nullptr;
         if (kind == kRowMix || kind < 0) {
-            CAPSP_TRY(ensure_mix(h, group_rows_for(nb), tn.border, view_upper, &mt));
+            CAPSP_TRY(ensure_mix(h, group_rows_for(nb), tn.border, &mt));
             if (kind < 0)
                 kind = mt->wo > 0.0 ? kRowMix : kRowWrtFst;
         }
-        CAPSP_CUDA(launch_fill_pending<T>(x + r0, h->n, nb, ld, h->d_ticket, 1,
-                                          r0 == 0 ? h->d_err : nullptr, st));
+        // the publication vector starts all-pending: the caller's x (natural
+        // schedule) or the position-ordered scratch (level schedule)
+        if (level)
+            CAPSP_CUDA(launch_fill_pending<T>((T *)h->d_xp, h->n, nb, nb, h->d_ticket, 1,
+                                              r0 == 0 ? h->d_err : nullptr, st));
+        else
+            CAPSP_CUDA(launch_fill_pending<T>(x + r0, h->n, nb, ld, h->d_ticket, 1,
+                                              r0 == 0 ? h->d_err : nullptr, st));
         RowArgs<T> a;
         a.ptr = h->d_ptr;
         a.idx = h->d_idx;
         a.val = (const T *)h->d_val;
         a.inv_diag = (const T *)h->d_inv;
+        a.perm = level ? h->d_perm : nullptr;
+        a.lptr = h->d_lptr;
+        a.lidx = h->d_lidx;
+        a.lval = (const T *)h->d_lval;
+        a.linv = (const T *)h->d_linv;
+        a.xp = (T *)h->d_xp;
+        a.ldp = nb;
         a.b = b + r0;
         a.x = x + r0;
         a.ld = ld;
@@ -541,6 +718,7 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs,
         a.err = h->d_err;
         a.wait = h->wait;
         a.stuck_row = h->stuck_row;
+        a.trace = r0 == 0 ? h->trace : nullptr;
         const bool prof = h->profiling && r0 == 0;
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k0, st));
@@ -607,7 +785,7 @@ static capsp_status_t enqueue_op(capsp_handle_t h, Op op, const T *in, T *out, c
     if (op == kOpTransposeGrad && h->format != CAPSP_FMT_CSR)
         return fail(CAPSP_ERR_UNSUPPORTED, "the fused transpose+gradient sweep needs a CSR handle");
     if (row_path)
-        return enqueue_rows<T>(h, in, out, nrhs, ld, transpose, tn, st);
+        return enqueue_rows<T>(h, in, out, nrhs, ld, tn, st);
     // column path: CSC solve (forward for lower) or CSR transpose (backward for lower)
     const int backward = transpose ? (h->uplo == CAPSP_LOWER) : (h->uplo == CAPSP_UPPER);
     return enqueue_cols<T>(h, in, out, nrhs, ld, backward, xf, grad, tn, st);
@@ -698,12 +876,16 @@ static capsp_status_t prepare(capsp_handle_t h, int nrhs, bool transpose)
 {
     const bool row_path = (h->format == CAPSP_FMT_CSR) != transpose;
     if (row_path) {
+        if (h->sched == CAPSP_SCHED_LEVEL) {
+            CAPSP_TRY(build_level(h));
+            CAPSP_TRY(ensure_xp(h, nrhs));
+        }
         const Tuning tn = current_tuning(h, nrhs);
         if (tn.kind == kRowMix || tn.kind < 0) {
             MixTable *mt = nullptr;
             for (int r0 = 0; r0 < nrhs; r0 += 32) {
                 const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
-                CAPSP_TRY(ensure_mix(h, group_rows_for(nb), tn.border, row_view_upper(h, transpose), &mt));
+                CAPSP_TRY(ensure_mix(h, group_rows_for(nb), tn.border, &mt));
             }
         }
         return CAPSP_OK;
@@ -781,14 +963,17 @@ extern "C" capsp_status_t capsp_autotune(capsp_handle_t h, const void *b, void *
         const int rs[3] = {1, 2, 4};
         const bool allow_thread = h->alg == CAPSP_ALG_AUTO || h->alg == CAPSP_ALG_WRTFST;
         const bool allow_mix = h->alg == CAPSP_ALG_AUTO || h->alg == CAPSP_ALG_MIX;
+        const int bpss[2] = {0, 2};
         if (allow_thread)
             for (int bl : blocks)
                 for (int r : rs)
-                    cands.push_back({kRowWrtFst, r, bl, 0, h->border});
+                    for (int bp : bpss)
+                        cands.push_back({kRowWrtFst, r, bl, bp, h->border});
         if (h->alg == CAPSP_ALG_TWOPART)
             for (int bl : blocks)
                 for (int r : rs)
-                    cands.push_back({kRowTwoPart, r, bl, 0, h->border});
+                    for (int bp : bpss)
+                        cands.push_back({kRowTwoPart, r, bl, bp, h->border});
         if (allow_mix) {
             const int borders[4] = {4, 8, 16, 32};
             for (int bl : blocks)
@@ -811,7 +996,7 @@ extern "C" capsp_status_t capsp_autotune(capsp_handle_t h, const void *b, void *
             MixTable *mt = nullptr;
             for (int r0 = 0; r0 < nrhs && st_all == CAPSP_OK; r0 += 32) {
                 const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
-                st_all = ensure_mix(h, group_rows_for(nb), tn.border, row_view_upper(h, false), &mt);
+                st_all = ensure_mix(h, group_rows_for(nb), tn.border, &mt);
             }
         }
         if (st_all != CAPSP_OK)
@@ -912,6 +1097,15 @@ extern "C" capsp_status_t capsp_set_profiling(capsp_handle_t h, int enable)
     return CAPSP_OK;
 }
 
+extern "C" capsp_status_t capsp_debug_trace(capsp_handle_t h, void *row_times_ns)
+{
+    if (!h)
+        return fail(CAPSP_ERR_INVALID, "handle is NULL");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    h->trace = (unsigned long long *)row_times_ns;
+    return CAPSP_OK;
+}
+
 extern "C" capsp_status_t capsp_last_kernel_ms(capsp_handle_t h, float *ms)
 {
     if (!h || !ms)
@@ -945,11 +1139,13 @@ extern "C" capsp_status_t capsp_get_info(capsp_handle_t h, capsp_info_t *info)
     info->rows_per_thread = tn.R;
     info->block_threads = tn.block;
     info->blocks_per_sm = tn.bps;
+    info->schedule = h->sched;
+    info->levels = h->levels;
     if (h->format == CAPSP_FMT_CSC) {
         info->algorithm = CAPSP_ALG_SYNCFREE_CSC;
     } else {
         int alg = h->alg;
-        auto mit = h->mix.find(32);
+        auto mit = h->mix.find(32 * 2 + (h->sched == CAPSP_SCHED_LEVEL ? 1 : 0));
         if (mit != h->mix.end() && mit->second.d) {
             info->mix_len = mit->second.len;
             info->warp_occupy = mit->second.wo;

@@ -77,6 +77,85 @@ __device__ __forceinline__ void st_relaxed(unsigned int *p, unsigned int v)
     asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// L2 eviction policies.  The matrix arrays are streamed once per solve and
+// marked evict_first; the publication vector (a few tens of MB that every
+// dependency poll and every publication touches) is marked evict_last, so the
+// streamed data does not push it out of the 129 MB L2 and a poll or a
+// publication never pays a DRAM round trip.
+__device__ __forceinline__ unsigned long long l2_policy_evict_first()
+{
+    unsigned long long p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ unsigned long long l2_policy_evict_last()
+{
+    unsigned long long p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// read-only streamed loads with an L2 policy
+__device__ __forceinline__ int ld_stream(const int *p, unsigned long long pol)
+{
+    int v;
+    asm("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+__device__ __forceinline__ double ld_stream(const double *p, unsigned long long pol)
+{
+    double v;
+    asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+__device__ __forceinline__ float ld_stream(const float *p, unsigned long long pol)
+{
+    float v;
+    asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+// relaxed gpu-scope poll / publication with an L2 policy
+// Polls carry no "memory" clobber: they must be re-issued every round
+// (volatile) but need not be ordered against the warp's shared-memory
+// traffic, and without the clobber consecutive polls go out back to back.
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long *p, unsigned long long pol)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.L2::cache_hint.b64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+__device__ __forceinline__ unsigned int ld_relaxed(const unsigned int *p, unsigned long long pol)
+{
+    unsigned int v;
+    asm volatile("ld.relaxed.gpu.global.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+__device__ __forceinline__ void st_relaxed(unsigned long long *p, unsigned long long v, unsigned long long pol)
+{
+    asm volatile("st.relaxed.gpu.global.L2::cache_hint.b64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
+}
+
+__device__ __forceinline__ void st_relaxed(unsigned int *p, unsigned int v, unsigned long long pol)
+{
+    asm volatile("st.relaxed.gpu.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+
+__device__ __forceinline__ void st_stream(unsigned long long *p, unsigned long long v, unsigned long long pol)
+{
+    asm volatile("st.global.L2::cache_hint.b64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
+}
+
+__device__ __forceinline__ void st_stream(unsigned int *p, unsigned int v, unsigned long long pol)
+{
+    asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+
 __device__ __forceinline__ unsigned long long global_timer_ns()
 {
     unsigned long long t;

@@ -16,10 +16,23 @@ namespace capsp {
 // row and the first entry of an upper row.
 template <typename T>
 struct RowArgs {
+    // natural solve order: the matrix arrays themselves
     const int *ptr;
     const int *idx;
     const T *val;
     const T *inv_diag;
+    // level schedule (perm != nullptr): everything indexed by schedule
+    // position k; row perm[k] has dependencies at positions
+    // lidx[lptr[k] .. lptr[k+1]) (ascending) with values lval[...], and
+    // publishes into the position-ordered scratch xp (element (k, r) at
+    // k*ldp + r) as well as into the caller's x.
+    const int *perm;
+    const int *lptr;
+    const int *lidx;
+    const T *lval;
+    const T *linv;
+    T *xp;
+    long long ldp;
     const T *b;
     T *x;
     long long ld;  // element (i, r) at i*ld + r
@@ -32,6 +45,7 @@ struct RowArgs {
     int *err;
     WaitCfg wait;
     int stuck_row;  // debug: this row never publishes (-1: none)
+    unsigned long long *trace;  // tracing, per row i: [4i] chunk taken, [4i+1] first poll, [4i+2] last dependency received, [4i+3] published (ns)
 };
 
 // Arguments of the column-driven solve (SyncFree CSC kernel, and the
@@ -89,6 +103,13 @@ cudaError_t launch_fill_pending(T *x, int n, int nrhs, long long ld, unsigned *t
 template <typename T>
 cudaError_t launch_inv_diag(const int *ptr, const T *val, T *inv, int n, int diag_last, int *bad,
                             cudaStream_t st);
+
+// level-schedule values: linv[p] = 1/val[diag_src[p]] and the pre-scaled
+// dependency values lval[k] = -val[dep_src[k]] * linv[p] for k in lptr[p]..lptr[p+1]
+// (records the first position with a zero or non-finite diagonal in *bad)
+template <typename T>
+cudaError_t launch_level_values(const int *lptr, const int *dep_src, const int *diag_src, int n,
+                                const T *val, T *lval, T *linv, int *bad, cudaStream_t st);
 
 template <typename T>
 cudaError_t launch_grad_val(const int *rowptr, const int *colidx, const T *y, const T *x,

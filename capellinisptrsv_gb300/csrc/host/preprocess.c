@@ -161,6 +161,106 @@ int capsp_row_levels(int n, const int *rowptr, const int *colidx, int *level, in
     return deepest;
 }
 
+/* Level schedule of a triangular matrix read row by row (rows of a CSR, or
+ * columns of a CSC read as rows of the transpose).  Solve order visits rows
+ * 0..n-1 (diagonal last, dependencies on smaller rows) or, with upper != 0,
+ * rows n-1..0 (diagonal first, dependencies on larger rows).  Every row gets
+ * level 1 + the deepest level among its dependencies; a stable counting sort
+ * by level gives order[k] (k-th row to solve) and position[row] = k.  Any
+ * order that lists dependencies first keeps the sync-free solve correct;
+ * this one puts rows that become ready together next to each other.
+ * level_start (n+2 ints, optional) receives the first position of every level.
+ * Returns the number of levels, or -1 on allocation failure. */
+int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *order, int *position,
+                         int *level_start)
+{
+    int *lev = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int *cnt = (int *)calloc((size_t)n + 2, sizeof(int));
+    if (!lev || !cnt) {
+        free(lev);
+        free(cnt);
+        return -1;
+    }
+    int deepest = 0;
+    for (int p = 0; p < n; ++p) {
+        const int i = upper ? n - 1 - p : p;
+        const int s = ptr[i] + (upper ? 1 : 0), e = ptr[i + 1] - (upper ? 0 : 1);
+        int lv = 1;
+        for (int j = s; j < e; ++j) {
+            const int q = upper ? n - 1 - idx[j] : idx[j];
+            if (lev[q] + 1 > lv)
+                lv = lev[q] + 1;
+        }
+        lev[p] = lv;
+        cnt[lv]++;
+        if (lv > deepest)
+            deepest = lv;
+    }
+    /* exclusive scan over levels 1..deepest: first position of each level */
+    int run = 0;
+    for (int l = 0; l <= deepest + 1; ++l) {
+        int c = cnt[l];
+        cnt[l] = run;
+        run += c;
+    }
+    if (level_start)
+        for (int l = 0; l <= deepest + 1; ++l)
+            level_start[l] = cnt[l];
+    for (int p = 0; p < n; ++p) {
+        const int i = upper ? n - 1 - p : p;
+        const int k = cnt[lev[p]]++;
+        order[k] = i;
+        position[i] = k;
+    }
+    free(lev);
+    free(cnt);
+    return deepest;
+}
+
+/* Dependency structure in schedule-position space: for position k (row
+ * order[k]) its dependencies' positions, ascending, in dep_idx[dep_ptr[k] ..
+ * dep_ptr[k+1]); dep_src gives the index of each dependency's value in the
+ * original arrays and diag_src[k] that of the row's diagonal.  dep_ptr has
+ * n+1 entries, dep_idx/dep_src nnz-n.  Returns 0 or -1 on a malformed row. */
+int capsp_level_layout(int n, const int *ptr, const int *idx, int upper, const int *order,
+                       const int *position, int *dep_ptr, int *dep_idx, int *dep_src, int *diag_src)
+{
+    dep_ptr[0] = 0;
+    for (int k = 0; k < n; ++k) {
+        const int i = order[k];
+        dep_ptr[k + 1] = dep_ptr[k] + (ptr[i + 1] - ptr[i] - 1);
+    }
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int k = 0; k < n; ++k) {
+        const int i = order[k];
+        const int s = ptr[i], e = ptr[i + 1];
+        const int d = upper ? s : e - 1;
+        if (idx[d] != i) {
+            bad = 1;
+            continue;
+        }
+        diag_src[k] = d;
+        int w = dep_ptr[k];
+        for (int j = s; j < e; ++j) {
+            if (j == d)
+                continue;
+            /* insertion into the ascending run [dep_ptr[k], w) */
+            const int q = position[idx[j]];
+            int u = w - 1;
+            while (u >= dep_ptr[k] && dep_idx[u] > q) {
+                dep_idx[u + 1] = dep_idx[u];
+                dep_src[u + 1] = dep_src[u];
+                --u;
+            }
+            dep_idx[u + 1] = q;
+            dep_src[u + 1] = j;
+            ++w;
+        }
+    }
+    return bad ? -1 : 0;
+}
+
 void capsp_indegree(int n, int nnz, const int *idx, int *indeg)
 {
     memset(indeg, 0, sizeof(int) * (size_t)(n > 0 ? n : 1));

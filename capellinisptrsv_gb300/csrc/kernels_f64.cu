@@ -10,6 +10,7 @@ template cudaError_t launch_col_solve<double>(const ColArgs<double> &, int, int,
 template cudaError_t launch_fill_pending<double>(double *, int, int, long long, unsigned *, int, int *,
                                               cudaStream_t);
 template cudaError_t launch_inv_diag<double>(const int *, const double *, double *, int, int, int *, cudaStream_t);
+template cudaError_t launch_level_values<double>(const int *, const int *, const int *, int, const double *, double *, double *, int *, cudaStream_t);
 template cudaError_t launch_grad_val<double>(const int *, const int *, const double *, const double *, double *, int,
                                           int, long long, int, cudaStream_t);
 

@@ -13,19 +13,28 @@
 //
 // GB300 design (what differs from the reference):
 //   * Persistent grid sized from the SM count and occupancy; a warp takes
-//     its next chunk of consecutive rows from one atomic ticket.  Rows are
-//     therefore started in solve order by warps that are already running, so
-//     the lowest unfinished row always has a running owner whose
-//     dependencies are finished: forward progress needs no assumption about
-//     block scheduling.  (The reference takes one ticket per thread and maps
-//     lanes from threadIdx, mix/...:32-45.)
+//     its next chunk of consecutive schedule positions from one atomic
+//     ticket.  Positions are therefore started in schedule order by warps
+//     that are already running, so the lowest unfinished position always has
+//     a running owner whose dependencies are finished: forward progress needs
+//     no assumption about block scheduling.  (The reference takes one ticket
+//     per thread and maps lanes from threadIdx, mix/...:32-45.)
+//   * Two schedules.  NATURAL visits rows in index order (no preprocessing,
+//     like the reference).  LEVEL visits rows sorted by dependency level
+//     (built at analysis): a warp's chunk then holds rows that become ready
+//     together, so no lane idles behind a row several levels deeper, far
+//     fewer rows need to be in flight, and chains through consecutive levels
+//     stay inside one warp.  LEVEL works in schedule-position space:
+//     dependencies are stored as positions and values are published into a
+//     position-ordered scratch vector (plus the caller's x).
 //   * Value-as-flag readiness (capsp_device.cuh): no flag array, no fence.
 //   * Dependencies inside the warp's own chunk are read from a per-warp
-//     shared-memory mirror of the chunk's x values instead of from L2.
-//   * Each lane fetches up to kBatch column indices and values of its row
-//     at once and keeps all of their polls in flight together.
-//   * Partial sums are accumulated in storage (column) order whatever the
-//     arrival order, so WRTFST and TWOPART produce bit-identical results.
+//     shared-memory mirror of the chunk's values instead of from L2.
+//   * Polling: the first sweep polls every dependency; afterwards only the
+//     newest pending one is polled until it lands, then the rest are swept.
+//   * Partial sums are accumulated in storage order whatever the arrival
+//     order, so repeated solves and the WRTFST / TWOPART schedules are
+//     bit-identical.
 //   * 1/diag is precomputed at analysis; x = (b - sum) * (1/diag).
 //   * Multi-RHS: G = next_pow2(nrhs) lanes share a row, one right-hand side
 //     each; every (row, rhs) element is published and polled independently.
@@ -39,179 +48,466 @@ namespace capsp {
 
 constexpr int kBatch = 8;  // dependencies one lane keeps in flight
 
-template <typename T, int G, bool TWO>
-__device__ __forceinline__ void thread_row(const RowArgs<T> &a, const int p, const int g,
-                                           const int lo, volatile typename VBits<T>::U *cache)
+// Where a row's data lives, for the natural and the level schedule.
+template <typename T, bool LEVEL>
+struct RowView {
+    int i;         // row index (output / b / trace)
+    int s, e;      // dependency range in idx/val
+    const int *idx;
+    const T *val;
+    T dinv;
+    typename VBits<T>::U *pub;  // publication vector (x or xp)
+    long long pld;              // its row stride
+    long long pslot;            // this row's slot in pub (row i or position p)
+
+    __device__ __forceinline__ RowView(const RowArgs<T> &a, int p, unsigned long long pol)
+    {
+        typedef typename VBits<T>::U U;
+        if (LEVEL) {
+            i = ld_stream(a.perm + p, pol);
+            s = ld_stream(a.lptr + p, pol);
+            e = ld_stream(a.lptr + p + 1, pol);
+            idx = a.lidx;
+            val = a.lval;
+            dinv = ld_stream(a.linv + p, pol);
+            pub = reinterpret_cast<U *>(a.xp);
+            pld = a.ldp;
+            pslot = p;
+        } else {
+            i = a.upper ? a.n - 1 - p : p;
+            s = ld_stream(a.ptr + i, pol);
+            e = ld_stream(a.ptr + i + 1, pol);
+            if (a.upper)
+                ++s;
+            else
+                --e;
+            idx = a.idx;
+            val = a.val;
+            dinv = ld_stream(a.inv_diag + i, pol);
+            pub = reinterpret_cast<U *>(a.x);
+            pld = a.ld;
+            pslot = i;
+        }
+    }
+    // schedule position of the dependency stored as c
+    __device__ __forceinline__ int pos_of(const RowArgs<T> &a, int c) const
+    {
+        return LEVEL ? c : (a.upper ? a.n - 1 - c : c);
+    }
+    // newest pending dependency: highest position (storage order ascends in
+    // position except for the natural upper view, where it descends)
+    __device__ __forceinline__ unsigned newest(const RowArgs<T> &a, unsigned pend) const
+    {
+        return (!LEVEL && a.upper) ? (pend & (0u - pend)) : (1u << (31 - __clz(pend)));
+    }
+};
+
+// L2 policies of one kernel launch (see capsp_device.cuh)
+struct L2Pol {
+    unsigned long long stream;  // evict_first: matrix arrays, b, the output x of the level schedule
+    unsigned long long keep;    // evict_last: the publication vector
+};
+
+template <typename T, bool LEVEL>
+__device__ __forceinline__ void publish(const RowArgs<T> &a, const RowView<T, LEVEL> &rv, int g,
+                                        typename VBits<T>::U ub, const L2Pol &pol)
+{
+    typedef typename VBits<T>::U U;
+    st_relaxed(rv.pub + (size_t)rv.pslot * (size_t)rv.pld + g, ub, pol.keep);
+    if (LEVEL)
+        st_stream(reinterpret_cast<U *>(a.x) + (size_t)rv.i * (size_t)a.ld + g, ub, pol.stream);
+}
+
+// Per-warp shared-memory slot storage: for each lane, the values and the
+// received dependency values of its current batch, so that the in-order fold
+// can run a data-dependent loop (a fully unrolled, predicated FMA chain would
+// wait ~64 cycles per slot on this GPU's FP64 pipe even when predicated off).
+template <typename T>
+struct Slots {
+    T *v;                          // dependency values, [t * 32 + lane]
+    typename VBits<T>::U *w;       // received x values
+    int *q;                        // dependency positions
+};
+
+// bytes of dynamic shared memory per warp: chunk mirror + slot storage
+template <typename T>
+__host__ __device__ constexpr size_t warp_smem_bytes(int R)
+{
+    return (size_t)32 * R * sizeof(typename VBits<T>::U) +
+           (size_t)kBatch * 32 * (sizeof(T) + sizeof(typename VBits<T>::U) + sizeof(int));
+}
+
+// Convergent chunk solve.  The warp's chunk holds schedule positions
+// [lo, lo + CH); in each pass over a sub-chunk of 32/G positions starting at
+// `sub`, lane (rl, g) owns the element (position p = sub + rl, rhs g).  All
+// lanes advance together in rounds, so a warp never splits into long-lived
+// divergent paths (which the hardware runs one at a time):
+//   A. every lane issues the polls it selected for dependencies before the
+//      chunk (relaxed gpu-scope loads), all in flight together;
+//   B. runs only when something changed: a ballot of the lanes that have
+//      published tells every lane whether a producer of one of its
+//      dependencies inside the sub-chunk has published; those values come
+//      from the shared-memory mirror; contributions are folded in storage
+//      order as soon as the ready prefix grows, so when the last dependency
+//      lands a single FMA remains; complete rows publish, and B repeats while
+//      lanes publish, so a chain through the sub-chunk resolves in one round;
+//   C. a round in which nothing moved backs off and checks the wait budget.
+// Level schedule: values are pre-scaled at analysis, x = b/d + sum (-v/d) x_j,
+// so no FP64 work is left after the last dependency but that FMA (one
+// warp-wide DFMA occupies an SM sub-partition's FP64 pipe for ~64 cycles).
+// TWO (the two-phase schedule of the reference's our2Part) polls the outside
+// dependencies one at a time in storage order.
+template <typename T, int G, bool TWO, bool LEVEL>
+__device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, const int sub, const int p,
+                                           const bool mine, const int g,
+                                           volatile typename VBits<T>::U *cache, const Slots<T> &sl,
+                                           const unsigned long long t_pick, const L2Pol &pol)
 {
     typedef VBits<T> VB;
     typedef typename VB::U U;
-    const int i = a.upper ? a.n - 1 - p : p;
-    int s = __ldg(a.ptr + i), e = __ldg(a.ptr + i + 1);
-    if (a.upper)
-        ++s;
-    else
-        --e;
-    const size_t xo = (size_t)i * (size_t)a.ld + (size_t)g;
-    const T bi = __ldg(a.b + xo);
-    const T dinv = __ldg(a.inv_diag + i);
-    const U *xb = reinterpret_cast<const U *>(a.x);
-    T acc = T(0);
-    bool aborted = false;
-    for (int j0 = s; j0 < e && !aborted; j0 += kBatch) {
-        const int cnt = min(kBatch, e - j0);
-        int c[kBatch];
-        T v[kBatch];
-        U w[kBatch];
+    const int lane = threadIdx.x & 31;
+    int i = 0, j0 = 0, e = 0;
+    const int *idxp = nullptr;
+    const T *valp = nullptr;
+    T dinv = T(0), bi = T(0), acc = T(0);
+    U *pub = nullptr;
+    long long pld = 0, pslot = 0;
+    if (mine) {
+        const RowView<T, LEVEL> rv(a, p, pol.stream);
+        i = rv.i;
+        j0 = rv.s;
+        e = rv.e;
+        idxp = rv.idx;
+        valp = rv.val;
+        dinv = rv.dinv;
+        pub = rv.pub;
+        pld = rv.pld;
+        pslot = rv.pslot;
+        bi = ld_stream(a.b + (size_t)i * (size_t)a.ld + g, pol.stream);
+        if (LEVEL)
+            acc = bi * dinv;  // x = b/d + sum (-v/d) x_j
+    }
+    int c[kBatch];                    // dependency index (position, or row in natural order)
+    unsigned pend = 0, ext = 0, need = 0;
+    int nacc = 0, cnt = 0;
+    auto load_batch = [&]() {
+        cnt = min(kBatch, e - j0);
+        pend = ext = need = 0;
+        nacc = 0;
 #pragma unroll
         for (int t = 0; t < kBatch; ++t) {
             c[t] = 0;
-            v[t] = T(0);
-            w[t] = 0;
             if (t < cnt) {
-                c[t] = __ldg(a.idx + j0 + t);
-                v[t] = __ldg(a.val + j0 + t);
-            }
-        }
-        unsigned pend = (1u << cnt) - 1u;
-        if (TWO) {
-            // phase 1: dependencies outside this warp's chunk, one at a time
-#pragma unroll
-            for (int t = 0; t < kBatch; ++t) {
-                if (!aborted && ((pend >> t) & 1u)) {
-                    const int q = a.upper ? a.n - 1 - c[t] : c[t];
-                    if (q < lo) {
-                        const U *src = xb + (size_t)c[t] * (size_t)a.ld + g;
-                        U u = ld_relaxed(src);
-                        Spin sp;
-                        while (u == VB::kPending) {
-                            if (sp.next(a.err, a.wait, i, c[t])) {
-                                aborted = true;
-                                break;
-                            }
-                            u = ld_relaxed(src);
-                        }
-                        w[t] = u;
-                        pend &= ~(1u << t);
-                    }
+                const int cc = ld_stream(idxp + j0 + t, pol.stream);
+                const int q = LEVEL ? cc : (a.upper ? a.n - 1 - cc : cc);
+                c[t] = cc;
+                sl.v[t * 32 + lane] = ld_stream(valp + j0 + t, pol.stream);
+                sl.q[t * 32 + lane] = q;
+                if (q < lo) {
+                    ext |= 1u << t;
+                    pend |= 1u << t;
+                } else if (q < sub) {  // earlier sub-chunk of this chunk: already in the mirror
+                    sl.w[t * 32 + lane] = cache[(q - lo) * G + g];
+                } else {
+                    pend |= 1u << t;
+                    need |= 1u << ((q - sub) * G + g);
                 }
             }
         }
-        // write-first: consume whichever dependencies are ready, re-poll the rest
-        Spin sp;
-        int waited = 0;
-        while (pend && !aborted) {
+    };
+    // fold the contributions of the ready prefix [nacc, first pending)
+    auto fold = [&]() {
+        const int lim = pend ? __ffs(pend) - 1 : cnt;
+        for (int t = nacc; t < lim; ++t)
+            acc = fma(sl.v[t * 32 + lane], VB::from(sl.w[t * 32 + lane]), acc);
+        nacc = lim;
+    };
+    bool done = !mine, published = !mine;
+    if (mine && j0 < e)
+        load_batch();
+    bool probe_only = false, aborted = false;
+    unsigned long long t_ready = 0;
+    Spin sp;
+    int waited = 0;
+    bool first = true;
+    unsigned long long t_first = 0;
+    if (a.trace != nullptr)
+        t_first = global_timer_ns();
+    for (;;) {
+        // ---- A: polls of dependencies before the chunk ---------------------
+        // The first round polls every outstanding dependency; afterwards each
+        // lane polls only its newest outstanding one until it lands, then
+        // sweeps the rest.  The two-phase schedule instead walks each lane's
+        // outside dependencies one at a time, oldest first.
+        bool changed = first;
+        first = false;
+        const unsigned ext_pend = done ? 0u : (pend & ext);
+        unsigned top = 0u;
+        if (TWO)
+            top = ext_pend & (0u - ext_pend);  // oldest outside dependency first
+        else if (ext_pend)
+            top = (!LEVEL && a.upper) ? (ext_pend & (0u - ext_pend)) : (1u << (31 - __clz(ext_pend)));
+        const bool sweep = !TWO && ext_pend != 0u && !probe_only;
+        if (!__any_sync(kFullMask, sweep)) {
+            // probe round (warp-uniform): one branch-free load per lane, the
+            // lane's newest (oldest for TWO) outside dependency; lanes with
+            // nothing outstanding read their own slot
+            const U *addr = pub + (size_t)pslot * (size_t)pld + g;
+#pragma unroll
+            for (int t = 0; t < kBatch; ++t)
+                if ((top >> t) & 1u)
+                    addr = pub + (size_t)c[t] * (size_t)pld + g;
+            const U u0 = mine ? ld_relaxed(addr, pol.keep) : VB::kPending;
+            if (top) {
+                if (u0 != VB::kPending) {
+#pragma unroll
+                    for (int t = 0; t < kBatch; ++t)
+                        if ((top >> t) & 1u)
+                            sl.w[t * 32 + lane] = u0;
+                    pend &= ~top;
+                    changed = true;
+                    probe_only = false;  // the newest landed: sweep the others next
+                    if (a.trace != nullptr && pend == 0 && j0 + kBatch >= e)
+                        t_ready = global_timer_ns();  // last dependency value received
+                } else {
+                    int w = 0;
+#pragma unroll
+                    for (int t = 0; t < kBatch; ++t)
+                        if ((top >> t) & 1u)
+                            w = c[t];
+                    waited = w;
+                }
+            }
+            if ((pend & ext) == 0u)
+                probe_only = false;
+        } else if (ext_pend) {
+            // sweep round: every outstanding outside dependency, all loads in
+            // flight together before any result is consumed (in-order issue
+            // would otherwise stall on the first result)
+            const unsigned sel = probe_only ? top : ext_pend;
+            U u[kBatch];
+#pragma unroll
+            for (int t = 0; t < kBatch; ++t)
+                u[t] = ((sel >> t) & 1u) ? ld_relaxed(pub + (size_t)c[t] * (size_t)pld + g, pol.keep)
+                                         : VB::kPending;
+            unsigned got = 0;
 #pragma unroll
             for (int t = 0; t < kBatch; ++t) {
-                if ((pend >> t) & 1u) {
-                    const int q = a.upper ? a.n - 1 - c[t] : c[t];
-                    const U u = (q >= lo) ? cache[(q - lo) * G + g]
-                                          : ld_relaxed(xb + (size_t)c[t] * (size_t)a.ld + g);
-                    if (u != VB::kPending) {
-                        w[t] = u;
-                        pend &= ~(1u << t);
+                if ((sel >> t) & 1u) {
+                    if (u[t] != VB::kPending) {
+                        sl.w[t * 32 + lane] = u[t];
+                        got |= 1u << t;
                     } else {
                         waited = c[t];
                     }
                 }
             }
-            if (pend && sp.next(a.err, a.wait, i, waited))
-                aborted = true;
+            pend &= ~got;
+            probe_only = (pend & ext) != 0 && !(got & top);
+            changed = changed || got != 0;
+            if (a.trace != nullptr && got != 0 && pend == 0 && j0 + kBatch >= e)
+                t_ready = global_timer_ns();  // last dependency value received
         }
-#pragma unroll
-        for (int t = 0; t < kBatch; ++t)
-            if (t < cnt)
-                acc = fma(v[t], VB::from(w[t]), acc);
-    }
-    U ub = aborted ? VB::kQNaN : VB::to((bi - acc) * dinv);
-    if (ub == VB::kPending)
-        ub = VB::kQNaN;
-    if (i != a.stuck_row) {
-        cache[(p - lo) * G + g] = ub;
-        st_relaxed(reinterpret_cast<U *>(a.x) + xo, ub);
+        // a lane whose current batch is complete but not yet folded also needs B
+        const bool progress = __any_sync(kFullMask, changed || (!done && pend == 0u));
+        // ---- B: in-sub-chunk pickup, fold, publish ------------------------
+        if (progress) {
+            for (;;) {
+                const unsigned pubmask = __ballot_sync(kFullMask, published);
+                bool moved = false;
+                if (!done) {
+                    if (need & pubmask) {
+                        unsigned m = pend & ~ext;
+                        while (m) {
+                            const int t = __ffs(m) - 1;
+                            m &= m - 1;
+                            const int q = sl.q[t * 32 + lane];
+                            if ((pubmask >> ((q - sub) * G + g)) & 1u) {
+                                sl.w[t * 32 + lane] = cache[(q - lo) * G + g];
+                                pend &= ~(1u << t);
+                            }
+                        }
+                        need &= ~pubmask;
+                    }
+                    if (nacc < cnt)
+                        fold();
+                    if (pend == 0 && nacc >= cnt) {
+                        j0 += kBatch;
+                        if (j0 < e) {
+                            load_batch();  // a row with more than kBatch dependencies
+                            probe_only = false;
+                            moved = true;
+                        } else {
+                            if (a.trace != nullptr && t_ready == 0)
+                                t_ready = global_timer_ns();
+                            U ub = VB::to(LEVEL ? acc : (bi - acc) * dinv);
+                            if (ub == VB::kPending)
+                                ub = VB::kQNaN;
+                            if (i != a.stuck_row) {
+                                cache[(p - lo) * G + g] = ub;
+                                st_relaxed(pub + (size_t)pslot * (size_t)pld + g, ub, pol.keep);
+                                if (LEVEL)
+                                    st_stream(reinterpret_cast<U *>(a.x) + (size_t)i * (size_t)a.ld + g, ub,
+                                              pol.stream);
+                                published = true;
+                            }
+                            if (a.trace != nullptr && g == 0) {
+                                a.trace[4 * (size_t)i] = t_pick;
+                                a.trace[4 * (size_t)i + 1] = t_first;
+                                a.trace[4 * (size_t)i + 2] = t_ready;
+                                a.trace[4 * (size_t)i + 3] = global_timer_ns();
+                            }
+                            done = true;
+                            moved = true;
+                        }
+                    }
+                }
+                __syncwarp();  // mirror stores visible to the next pickup
+                // another pass can only help a lane that still waits on a
+                // dependency inside the sub-chunk
+                if (!__any_sync(kFullMask, moved) ||
+                    !__any_sync(kFullMask, !done && (pend == 0u || (pend & ~ext) != 0u)))
+                    break;
+            }
+        }
+        if (__all_sync(kFullMask, done))
+            break;
+        // ---- C: back off when nothing moved; bounded wait -----------------
+        if (!progress) {
+            if (sp.next(a.err, a.wait, i, waited))
+                aborted = true;
+        } else {
+            sp.it = 0;
+        }
+        if (__any_sync(kFullMask, aborted)) {
+            // give up: unfinished rows publish a quiet NaN so their dependants end
+            if (!done && i != a.stuck_row) {
+                cache[(p - lo) * G + g] = VB::kQNaN;
+                st_relaxed(pub + (size_t)pslot * (size_t)pld + g, VB::kQNaN, pol.keep);
+                if (LEVEL)
+                    st_stream(reinterpret_cast<U *>(a.x) + (size_t)i * (size_t)a.ld + g, VB::kQNaN, pol.stream);
+            }
+            __syncwarp();
+            break;
+        }
     }
 }
 
 // One heavy row per warp: 32/G slices of the row's entries x G right-hand
-// sides; slices are reduced with butterfly shuffles.
-template <typename T, int G>
-__device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const int sl,
-                                         const int g)
+// sides, advanced in convergent rounds; slices are reduced with butterfly
+// shuffles once every lane has consumed its entries.
+template <typename T, int G, bool LEVEL>
+__device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const int sl_idx, const int g,
+                                         const Slots<T> &sl, const L2Pol &pol)
 {
     constexpr int NS = 32 / G;
     typedef VBits<T> VB;
     typedef typename VB::U U;
-    const int i = a.upper ? a.n - 1 - p : p;
-    int s = __ldg(a.ptr + i), e = __ldg(a.ptr + i + 1);
-    if (a.upper)
-        ++s;
-    else
-        --e;
+    const int lane = threadIdx.x & 31;
+    const RowView<T, LEVEL> rv(a, p, pol.stream);
+    const int i = rv.i;
     const bool active = g < a.nrhs;
-    const size_t xo = (size_t)i * (size_t)a.ld + (size_t)g;
-    T bi = T(0), dinv = T(0);
-    if (active && sl == 0) {
-        bi = __ldg(a.b + xo);
-        dinv = __ldg(a.inv_diag + i);
-    }
-    const U *xb = reinterpret_cast<const U *>(a.x);
+    T bi = T(0);
+    if (active && sl_idx == 0)
+        bi = ld_stream(a.b + (size_t)i * (size_t)a.ld + g, pol.stream);
+    const U *pb = rv.pub;
     T acc = T(0);
-    bool aborted = false;
-    if (active) {
-        for (int j0 = s + sl; j0 < e && !aborted; j0 += NS * kBatch) {
-            int c[kBatch];
-            T v[kBatch];
-            U w[kBatch];
-            unsigned pend = 0;
+    int c[kBatch];
+    unsigned pend = 0;
+    int cnt = 0;
+    int j0 = rv.s + sl_idx;
+    auto load_batch = [&]() {
+        pend = 0;
+        cnt = 0;
 #pragma unroll
-            for (int t = 0; t < kBatch; ++t) {
-                const int j = j0 + t * NS;
-                c[t] = 0;
-                v[t] = T(0);
-                w[t] = 0;
-                if (j < e) {
-                    c[t] = __ldg(a.idx + j);
-                    v[t] = __ldg(a.val + j);
-                    pend |= 1u << t;
-                }
+        for (int t = 0; t < kBatch; ++t) {
+            const int j = j0 + t * NS;
+            c[t] = 0;
+            if (j < rv.e) {
+                c[t] = ld_stream(rv.idx + j, pol.stream);
+                sl.v[t * 32 + lane] = ld_stream(rv.val + j, pol.stream);
+                pend |= 1u << t;
+                ++cnt;
             }
-            const unsigned have = pend;
-            Spin sp;
-            int waited = 0;
-            while (pend && !aborted) {
-#pragma unroll
-                for (int t = 0; t < kBatch; ++t) {
-                    if ((pend >> t) & 1u) {
-                        const U u = ld_relaxed(xb + (size_t)c[t] * (size_t)a.ld + g);
-                        if (u != VB::kPending) {
-                            w[t] = u;
-                            pend &= ~(1u << t);
-                        } else {
-                            waited = c[t];
-                        }
-                    }
-                }
-                if (pend && sp.next(a.err, a.wait, i, waited))
-                    aborted = true;
-            }
+        }
+    };
+    bool done = !active || j0 >= rv.e;
+    if (!done)
+        load_batch();
+    bool probe_only = false, aborted = false;
+    Spin sp;
+    int waited = 0;
+    for (;;) {
+        bool progress = false;
+        if (!done) {
+            const unsigned top = rv.newest(a, pend);
+            const unsigned sel = probe_only ? top : pend;
+            U u[kBatch];
 #pragma unroll
             for (int t = 0; t < kBatch; ++t)
-                if ((have >> t) & 1u)
-                    acc = fma(v[t], VB::from(w[t]), acc);
+                u[t] = ((sel >> t) & 1u) ? ld_relaxed(pb + (size_t)c[t] * (size_t)rv.pld + g, pol.keep)
+                                         : VB::kPending;
+            unsigned got = 0;
+#pragma unroll
+            for (int t = 0; t < kBatch; ++t) {
+                if ((sel >> t) & 1u) {
+                    if (u[t] != VB::kPending) {
+                        sl.w[t * 32 + lane] = u[t];
+                        got |= 1u << t;
+                    } else {
+                        waited = c[t];
+                    }
+                }
+            }
+            pend &= ~got;
+            probe_only = pend != 0 && !(got & top);
+            progress = got != 0;
+            if (pend == 0) {
+                for (int t = 0; t < cnt; ++t)
+                    acc = fma(sl.v[t * 32 + lane], VB::from(sl.w[t * 32 + lane]), acc);
+                j0 += NS * kBatch;
+                if (j0 < rv.e) {
+                    load_batch();
+                    probe_only = false;
+                } else {
+                    done = true;
+                }
+            }
         }
+        if (__all_sync(kFullMask, done))
+            break;
+        if (!__any_sync(kFullMask, progress)) {
+            if (sp.next(a.err, a.wait, i, waited))
+                aborted = true;
+        } else {
+            sp.it = 0;
+        }
+        if (__any_sync(kFullMask, aborted))
+            break;
     }
+    aborted = __any_sync(kFullMask, aborted);
 #pragma unroll
     for (int off = 16; off >= G; off >>= 1)
         acc += __shfl_xor_sync(kFullMask, acc, off);
-    aborted = __any_sync(kFullMask, aborted);
-    if (sl == 0 && active && i != a.stuck_row) {
-        U ub = aborted ? VB::kQNaN : VB::to((bi - acc) * dinv);
+    unsigned long long t_ready = 0;
+    if (a.trace != nullptr)
+        t_ready = global_timer_ns();
+    if (sl_idx == 0 && active && i != a.stuck_row) {
+        // level schedule: values are pre-scaled (x = b/d + sum), else x = (b - sum)/d
+        U ub = aborted ? VB::kQNaN : VB::to(LEVEL ? fma(bi, rv.dinv, acc) : (bi - acc) * rv.dinv);
         if (ub == VB::kPending)
             ub = VB::kQNaN;
-        st_relaxed(reinterpret_cast<U *>(a.x) + xo, ub);
+        publish<T, LEVEL>(a, rv, g, ub, pol);
+    }
+    if (a.trace != nullptr && sl_idx == 0 && g == 0) {
+        a.trace[4 * (size_t)i] = t_ready;
+        a.trace[4 * (size_t)i + 1] = t_ready;
+        a.trace[4 * (size_t)i + 2] = t_ready;
+        a.trace[4 * (size_t)i + 3] = global_timer_ns();
     }
 }
 
-template <typename T, int G, int R, int KIND>
+template <typename T, int G, int R, int KIND, bool LEVEL>
 __global__ void __launch_bounds__(512) row_solve_kernel(const RowArgs<T> a)
 {
     typedef typename VBits<T>::U U;
@@ -219,8 +515,17 @@ __global__ void __launch_bounds__(512) row_solve_kernel(const RowArgs<T> a)
     constexpr int CH = RPW * R;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
-    volatile U *cache = reinterpret_cast<volatile U *>(smem_raw) + (size_t)(threadIdx.x >> 5) * (32 * R);
+    const int wib = threadIdx.x >> 5;
+    unsigned char *wbase = smem_raw + (size_t)wib * warp_smem_bytes<T>(R);
+    volatile U *cache = reinterpret_cast<volatile U *>(wbase);
+    Slots<T> sl;
+    sl.v = reinterpret_cast<T *>(wbase + (size_t)32 * R * sizeof(U));
+    sl.w = reinterpret_cast<U *>(sl.v + kBatch * 32);
+    sl.q = reinterpret_cast<int *>(sl.w + kBatch * 32);
     const int rl = lane / G, g = lane % G;
+    L2Pol pol;
+    pol.stream = l2_policy_evict_first();
+    pol.keep = l2_policy_evict_last();
     for (;;) {
         unsigned tk = 0, stop = 0;
         if (lane == 0) {
@@ -231,6 +536,7 @@ __global__ void __launch_bounds__(512) row_solve_kernel(const RowArgs<T> a)
         stop = __shfl_sync(kFullMask, stop, 0);
         if (stop)
             break;
+        const unsigned long long t_pick = a.trace != nullptr ? global_timer_ns() : 0ull;
         if (KIND != kRowMix) {
             if (tk >= (unsigned)a.n)
                 break;
@@ -241,25 +547,26 @@ __global__ void __launch_bounds__(512) row_solve_kernel(const RowArgs<T> a)
             __syncwarp();
 #pragma unroll 1
             for (int r = 0; r < R; ++r) {
-                const int p = lo + r * RPW + rl;
-                if (p < a.n && g < a.nrhs)
-                    thread_row<T, G, KIND == kRowTwoPart>(a, p, g, lo, cache);
+                const int sub = lo + r * RPW;
+                const int p = sub + rl;
+                chunk_rows<T, G, KIND == kRowTwoPart, LEVEL>(a, lo, sub, p, p < a.n && g < a.nrhs, g, cache, sl,
+                                                             t_pick, pol);
             }
             __syncwarp();
         } else {
             if (tk + 1u >= (unsigned)a.table_len)
                 break;
-            const int lo = __ldg(a.table + tk), hi = __ldg(a.table + tk + 1);
+            const int lo = ld_stream(a.table + tk, pol.stream), hi = ld_stream(a.table + tk + 1, pol.stream);
             if (hi - lo > 1) {
                 cache[lane] = VBits<T>::kPending;
                 __syncwarp();
                 const int p = lo + rl;
-                if (p < hi && g < a.nrhs)
-                    thread_row<T, G, false>(a, p, g, lo, cache);
+                chunk_rows<T, G, false, LEVEL>(a, lo, lo, p, p < hi && g < a.nrhs, g, cache, sl, t_pick, pol);
                 __syncwarp();
             } else {
-                warp_row<T, G>(a, lo, rl, g);
+                warp_row<T, G, LEVEL>(a, lo, rl, g, sl, pol);
             }
+            __syncwarp();
         }
     }
 }
@@ -268,15 +575,21 @@ __global__ void __launch_bounds__(512) row_solve_kernel(const RowArgs<T> a)
 // launch helpers
 // ---------------------------------------------------------------------------
 
-template <typename T, int G, int R, int KIND>
+template <typename T, int G, int R, int KIND, bool LEVEL>
 static cudaError_t launch_row_impl(const RowArgs<T> &a, int block, int bps, int num_sms,
                                    cudaStream_t st)
 {
     constexpr int RPW = 32 / G;
-    auto kern = row_solve_kernel<T, G, R, KIND>;
-    const size_t smem = (size_t)(block / 32) * 32 * R * sizeof(typename VBits<T>::U);
+    auto kern = row_solve_kernel<T, G, R, KIND, LEVEL>;
+    const size_t smem = (size_t)(block / 32) * warp_smem_bytes<T>(R);
+    cudaError_t e = cudaSuccess;
+    if (smem > 48 * 1024) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+    }
     int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, smem);
     if (e != cudaSuccess)
         return e;
     if (occ < 1)
@@ -294,27 +607,41 @@ static cudaError_t launch_row_impl(const RowArgs<T> &a, int block, int bps, int 
     return cudaGetLastError();
 }
 
-template <typename T, int G>
+template <typename T, int G, bool LEVEL>
 static cudaError_t launch_row_g(const RowArgs<T> &a, int kind, int R, int block, int bps,
                                 int num_sms, cudaStream_t st)
 {
     if (kind == kRowMix)
-        return launch_row_impl<T, G, 1, kRowMix>(a, block, bps, num_sms, st);
+        return launch_row_impl<T, G, 1, kRowMix, LEVEL>(a, block, bps, num_sms, st);
     // the two-phase schedule is the reference's single-RHS design; multi-RHS
     // launches use the write-first schedule
     if constexpr (G == 1) {
         if (kind == kRowTwoPart) {
             switch (R) {
-            case 4: return launch_row_impl<T, G, 4, kRowTwoPart>(a, block, bps, num_sms, st);
-            case 2: return launch_row_impl<T, G, 2, kRowTwoPart>(a, block, bps, num_sms, st);
-            default: return launch_row_impl<T, G, 1, kRowTwoPart>(a, block, bps, num_sms, st);
+            case 4: return launch_row_impl<T, G, 4, kRowTwoPart, LEVEL>(a, block, bps, num_sms, st);
+            case 2: return launch_row_impl<T, G, 2, kRowTwoPart, LEVEL>(a, block, bps, num_sms, st);
+            default: return launch_row_impl<T, G, 1, kRowTwoPart, LEVEL>(a, block, bps, num_sms, st);
             }
         }
     }
     switch (R) {
-    case 4: return launch_row_impl<T, G, 4, kRowWrtFst>(a, block, bps, num_sms, st);
-    case 2: return launch_row_impl<T, G, 2, kRowWrtFst>(a, block, bps, num_sms, st);
-    default: return launch_row_impl<T, G, 1, kRowWrtFst>(a, block, bps, num_sms, st);
+    case 4: return launch_row_impl<T, G, 4, kRowWrtFst, LEVEL>(a, block, bps, num_sms, st);
+    case 2: return launch_row_impl<T, G, 2, kRowWrtFst, LEVEL>(a, block, bps, num_sms, st);
+    default: return launch_row_impl<T, G, 1, kRowWrtFst, LEVEL>(a, block, bps, num_sms, st);
+    }
+}
+
+template <typename T, bool LEVEL>
+static cudaError_t launch_row_sched(const RowArgs<T> &a, int kind, int rows_per_thread, int block,
+                                    int blocks_per_sm, int num_sms, cudaStream_t st)
+{
+    switch (lanes_for_rhs(a.nrhs)) {
+    case 1: return launch_row_g<T, 1, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
+    case 2: return launch_row_g<T, 2, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
+    case 4: return launch_row_g<T, 4, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
+    case 8: return launch_row_g<T, 8, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
+    case 16: return launch_row_g<T, 16, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
+    default: return launch_row_g<T, 32, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
     }
 }
 
@@ -322,18 +649,14 @@ template <typename T>
 cudaError_t launch_row_solve(const RowArgs<T> &a, int kind, int rows_per_thread, int block,
                              int blocks_per_sm, int num_sms, cudaStream_t st)
 {
-    switch (lanes_for_rhs(a.nrhs)) {
-    case 1: return launch_row_g<T, 1>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
-    case 2: return launch_row_g<T, 2>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
-    case 4: return launch_row_g<T, 4>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
-    case 8: return launch_row_g<T, 8>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
-    case 16: return launch_row_g<T, 16>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
-    default: return launch_row_g<T, 32>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
-    }
+    if (a.perm != nullptr)
+        return launch_row_sched<T, true>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
+    return launch_row_sched<T, false>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
 }
 
 // ---------------------------------------------------------------------------
-// fill x with the pending pattern, reset ticket counters and the error word
+// fill the publication vector with the pending pattern, reset ticket
+// counters and the error word
 // ---------------------------------------------------------------------------
 
 template <typename U>
@@ -393,6 +716,42 @@ cudaError_t launch_fill_pending(T *x, int n, int nrhs, long long ld, unsigned *t
         blocks = 1;
     fill_pending_kernel<U><<<(unsigned)blocks, 256, 0, st>>>(reinterpret_cast<U *>(x), n, nrhs, ld,
                                                             pat, p16, ticket, nticket, err);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// level-schedule values
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void level_values_kernel(const int *__restrict__ lptr, const int *__restrict__ dep_src,
+                                    const int *__restrict__ diag_src, int n, const T *__restrict__ val,
+                                    T *__restrict__ lval, T *__restrict__ linv, int *bad)
+{
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long p = tid; p < n; p += stride) {
+        const T dg = val[diag_src[p]];
+        if (!(dg != T(0)) || !isfinite(dg))
+            atomicMin(bad, (int)p);
+        const T d = T(1) / dg;
+        linv[p] = d;
+        // pre-scaled dependencies: x_p = b/d_p + sum (-v/d_p) x_q
+        for (int k = lptr[p]; k < lptr[p + 1]; ++k)
+            lval[k] = -val[dep_src[k]] * d;
+    }
+}
+
+template <typename T>
+cudaError_t launch_level_values(const int *lptr, const int *dep_src, const int *diag_src, int n,
+                                const T *val, T *lval, T *linv, int *bad, cudaStream_t st)
+{
+    long long blocks = ((long long)n + 255) / 256;
+    if (blocks > 8192)
+        blocks = 8192;
+    if (blocks < 1)
+        blocks = 1;
+    level_values_kernel<T><<<(unsigned)blocks, 256, 0, st>>>(lptr, dep_src, diag_src, n, val, lval, linv, bad);
     return cudaGetLastError();
 }
 

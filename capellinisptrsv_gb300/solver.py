@@ -194,7 +194,7 @@ class TriangularSolver:
 
     def __init__(self, rowptr, colidx, val, *, n: Optional[int] = None, fmt: str = "csr",
                  uplo: str = "lower", algorithm: str = "auto", validate: bool = True,
-                 sys_rowoff=None):
+                 sys_rowoff=None, schedule: Optional[str] = None):
         fmt_code = {"csr": N.FMT_CSR, "csc": N.FMT_CSC}[fmt]
         uplo_code = {"lower": N.LOWER, "upper": N.UPPER}[uplo]
         n = int(n if n is not None else len(rowptr) - 1)
@@ -228,6 +228,8 @@ class TriangularSolver:
                                      fmt_code, uplo_code, flags, C.byref(h))
         N.check(st)
         self._h = h
+        if schedule is not None:
+            self.set_schedule(schedule)
         if algorithm != "auto":
             self.set_algorithm(algorithm)
 
@@ -256,17 +258,29 @@ class TriangularSolver:
     def set_algorithm(self, algorithm: str) -> None:
         N.check(N.lib.capsp_set_algorithm(self._h, self._ALGS[algorithm]))
 
+    def set_schedule(self, schedule: str) -> None:
+        """'level' (rows sorted by dependency level, the default) or 'natural' (row order)."""
+        N.check(N.lib.capsp_set_schedule(self._h, {"natural": N.SCHED_NATURAL, "level": N.SCHED_LEVEL}[schedule]))
+
     def set_mix_border(self, border: int) -> None:
         N.check(N.lib.capsp_set_mix_border(self._h, int(border)))
 
     def set_tuning(self, rows_per_thread: int = 2, block: int = 256, blocks_per_sm: int = 0) -> None:
         N.check(N.lib.capsp_set_tuning(self._h, rows_per_thread, block, blocks_per_sm))
 
+    def set_backoff(self, sleep_max_ns: int) -> None:
+        N.check(N.lib.capsp_set_backoff(self._h, int(sleep_max_ns)))
+
     def set_timeout(self, seconds: float) -> None:
         N.check(N.lib.capsp_set_timeout(self._h, int(seconds * 1e9)))
 
     def debug_stuck_row(self, row: int, timeout_s: float = 0.0) -> None:
         N.check(N.lib.capsp_debug_set_stuck_row(self._h, int(row), int(timeout_s * 1e9)))
+
+    def trace(self, buf=None) -> None:
+        """Per-row timing trace into a CUDA int64 tensor of 4*n entries (None: off)."""
+        N.check(N.lib.capsp_debug_trace(self._h, _ptr(buf)))
+        self._trace_buf = buf
 
     def reserve(self, max_nrhs: int) -> None:
         N.check(N.lib.capsp_reserve(self._h, int(max_nrhs)))
@@ -290,6 +304,18 @@ class TriangularSolver:
         """set_values only if `val` is not the tensor (and version) already bound."""
         if (val.data_ptr(), val._version) != self._val_key:
             self.set_values(val)
+
+    def refresh_values(self, val=None, stream=None) -> None:
+        """Stream-ordered: borrow `val` (device handles) and recompute 1/diag, no sync.
+
+        Catches in-place changes that bypass the version counter (``.data`` writes)."""
+        if not self.on_device:
+            raise ValueError("refresh_values needs a solver built from CUDA tensors; use set_values")
+        if val is not None:
+            val = val.contiguous()
+            self._keep[2] = val
+            self._val_key = (val.data_ptr(), val._version)
+        N.check(N.lib.capsp_refresh_values(self._h, _ptr(val), C.c_void_p(_current_stream(stream))))
 
     # -- vectors --------------------------------------------------------------
     def _vec(self, t, name):
@@ -504,6 +530,36 @@ def row_levels(n, rowptr, colidx):
     counts = np.empty(n + 1, dtype=np.int32)
     deepest = N.lib.capsp_row_levels(int(n), _ptr(rowptr), _ptr(colidx), _ptr(level), _ptr(counts))
     return int(deepest), level, counts[: deepest + 1]
+
+
+def level_schedule(n, rowptr, colidx, upper: bool = False):
+    """Level order of the solve -> (levels, order, position, level_start)."""
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    colidx = np.ascontiguousarray(colidx, np.int32)
+    order = np.empty(n, np.int32)
+    position = np.empty(n, np.int32)
+    start = np.empty(n + 2, np.int32)
+    levels = N.lib.capsp_level_schedule(int(n), _ptr(rowptr), _ptr(colidx), int(bool(upper)), _ptr(order),
+                                        _ptr(position), _ptr(start))
+    if levels < 0:
+        raise MemoryError("level schedule allocation failed")
+    return int(levels), order, position, start[: levels + 2].copy()
+
+
+def level_layout(n, rowptr, colidx, order, position, upper: bool = False):
+    """Dependencies in schedule-position space -> (dep_ptr, dep_idx, dep_src, diag_src)."""
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    colidx = np.ascontiguousarray(colidx, np.int32)
+    nd = len(colidx) - n
+    dep_ptr = np.empty(n + 1, np.int32)
+    dep_idx = np.empty(max(nd, 1), np.int32)
+    dep_src = np.empty(max(nd, 1), np.int32)
+    diag_src = np.empty(n, np.int32)
+    rc = N.lib.capsp_level_layout(int(n), _ptr(rowptr), _ptr(colidx), int(bool(upper)), _ptr(order), _ptr(position),
+                                  _ptr(dep_ptr), _ptr(dep_idx), _ptr(dep_src), _ptr(diag_src))
+    if rc != 0:
+        raise ValueError("misplaced diagonal")
+    return dep_ptr, dep_idx[:nd], dep_src[:nd], diag_src
 
 
 def matrix_transposition(m, n, nnz, rowptr, colidx, val):

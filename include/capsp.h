@@ -82,6 +82,13 @@ typedef enum capsp_algorithm {
     CAPSP_ALG_SYNCFREE_CSC = 4 /* warp per column with left_sum atomics (CUDA/SyncFree_csc) */
 } capsp_algorithm_t;
 
+/* Order in which the row-driven kernels start rows.  Any order that lists a
+ * row after its dependencies keeps the solve synchronization-free. */
+typedef enum capsp_schedule {
+    CAPSP_SCHED_NATURAL = 0, /* row index order, no preprocessing (the reference's order) */
+    CAPSP_SCHED_LEVEL = 1    /* rows sorted by dependency level, built at analysis (default) */
+} capsp_schedule_t;
+
 /* capsp_analyse flags */
 #define CAPSP_DEVICE_POINTERS 0x1u /* ptr/idx/val are device pointers; the handle borrows them */
 #define CAPSP_SKIP_VALIDATION 0x2u /* trust the structure (no host/device structure check) */
@@ -104,6 +111,8 @@ typedef struct capsp_info {
     int block_threads;
     int blocks_per_sm;
     int num_sms;
+    int schedule;           /* capsp_schedule_t of the row-driven kernels */
+    int levels;             /* dependency levels (0 until a level schedule was built) */
 } capsp_info_t;
 
 /* ------------------------------------------------------------------------ */
@@ -137,12 +146,24 @@ capsp_status_t capsp_batched_create(int nsys, const int *sys_rowoff, int n, int 
  * device pointer for CAPSP_DEVICE_POINTERS handles (borrowed), else host. */
 capsp_status_t capsp_set_values(capsp_handle_t h, const void *val);
 
+/* Stream-ordered variant for CAPSP_DEVICE_POINTERS handles: borrow val (or,
+ * with val = NULL, keep the current pointer) and recompute 1/diag on `stream`
+ * without synchronising.  Meant for values that change between solves, e.g.
+ * parameters updated in place by an optimiser; a zero diagonal then shows up
+ * as inf/NaN in the results instead of an error code. */
+capsp_status_t capsp_refresh_values(capsp_handle_t h, const void *val, void *stream);
+
 capsp_status_t capsp_destroy(capsp_handle_t h);
 
 capsp_status_t capsp_get_info(capsp_handle_t h, capsp_info_t *info);
 
 /* Choose the row-driven algorithm for CSR handles (capsp_algorithm_t). */
 capsp_status_t capsp_set_algorithm(capsp_handle_t h, int algorithm);
+
+/* Row-driven schedule (capsp_schedule_t).  CAPSP_SCHED_LEVEL builds the level
+ * order on first use if capsp_analyse did not (CSC handles build it for their
+ * transposed solves); the build is host work proportional to nnz. */
+capsp_status_t capsp_set_schedule(capsp_handle_t h, int schedule);
 
 /* Mix selector threshold: 32-row groups whose mean nnz/row is >= border go
  * warp-per-row (the reference hard-codes 10, mix/spts_syncfree_cuda_csr_wrt.h:188). */
@@ -155,6 +176,10 @@ capsp_status_t capsp_set_tuning(capsp_handle_t h, int rows_per_thread,
 
 /* Budget for any single device dependency wait (default 10 s). */
 capsp_status_t capsp_set_timeout(capsp_handle_t h, uint64_t timeout_ns);
+
+/* Ceiling of the exponential __nanosleep backoff between polls of a pending
+ * dependency (default 256 ns; 0 = never sleep). */
+capsp_status_t capsp_set_backoff(capsp_handle_t h, unsigned sleep_max_ns);
 
 /* Solve op(A) X = B for nrhs right-hand sides (device pointers, element
  * (i,r) at i*ld + r, ld >= nrhs).  x must not alias b.  Stream-ordered,
@@ -216,6 +241,14 @@ capsp_status_t capsp_graph_solve(capsp_handle_t h, const void *b, void *x, int n
  * the fill of x and the scratch resets are excluded. */
 capsp_status_t capsp_set_profiling(capsp_handle_t h, int enable);
 capsp_status_t capsp_last_kernel_ms(capsp_handle_t h, float *ms);
+
+/* Tracing: with a device buffer of 4*n uint64 (NULL switches it off), every
+ * row-driven solve records per row i the global-timer nanoseconds at which its
+ * warp took the row ([4i]), first polled its dependencies ([4i+1]), had
+ * received the last of them ([4i+2]) and published its value ([4i+3]).
+ * A row's receipt minus its last dependency's publication is the
+ * dependency-hop latency. */
+capsp_status_t capsp_debug_trace(capsp_handle_t h, void *row_times_ns);
 
 /* Device properties used for launch sizing (SM count of the current device). */
 capsp_status_t capsp_device_sms(int *num_sms);
@@ -358,6 +391,23 @@ void matrix_warp4_f32(const int m, const int n, const int nnz, const int *csrRow
  * for upper-triangular matrices).  Returns the table length. */
 int capsp_mix_table(int n, const int *rowptr, int upper, int group_rows, int border,
                     int *table, double *warp_occupy, double *element_occupy);
+
+/* Level schedule of a triangular matrix read row by row in solve order
+ * (rows 0..n-1 with the diagonal last, or with upper != 0 rows n-1..0 with the
+ * diagonal first): level = 1 + deepest dependency level (the recurrence of
+ * matrix_layer); order[k] = k-th row of a stable sort by level, position =
+ * its inverse; level_start (optional, n+2 ints) = first position of each
+ * level.  Returns the level count or -1. */
+int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *order,
+                         int *position, int *level_start);
+
+/* Dependencies of every schedule position as positions (ascending), with the
+ * source index of each dependency value (dep_src) and of each diagonal
+ * (diag_src) in the original arrays.  dep_ptr: n+1; dep_idx, dep_src: nnz-n;
+ * diag_src: n.  Returns 0 or -1 when a diagonal is misplaced. */
+int capsp_level_layout(int n, const int *ptr, const int *idx, int upper, const int *order,
+                       const int *position, int *dep_ptr, int *dep_idx, int *dep_src,
+                       int *diag_src);
 
 /* In-degree analyser: histogram of idx (CUDA/SyncFree_csc/spts_syncfree_cuda2.h:10-21,
  * openCL/SynFree_csc/sptrsv_syncfree_serialref.h:6-23). */

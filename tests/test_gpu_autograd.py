@@ -61,6 +61,7 @@ def test_central_finite_differences_64_directions():
     (0.5 * ((x - t(xstar)) ** 2).sum()).backward()
     gval, gb = val.grad.cpu().numpy(), bt.grad.cpu().numpy()
     h = 1e-6
+    eps = np.finfo(np.float64).eps
     worst = 0.0
     for d in range(64):
         dv = rng.standard_normal(m.nnz)
@@ -69,9 +70,12 @@ def test_central_finite_differences_64_directions():
         fm = loss_of(t(m.val - h * dv), t(b - h * db))
         fd = (fp - fm) / (2 * h)
         an = float(np.dot(gval, dv) + np.sum(gb * db))
-        worst = max(worst, abs(fd - an) / max(1.0, abs(an)))
-    print(f"worst FD relative mismatch over 64 directions: {worst:.3e}")
-    assert worst < 1e-5
+        # central differences carry round-off ~ eps*|loss|/h (here |loss| ~ 1e5,
+        # so ~0.04 absolute) plus O(h^2) truncation; allow 8x that floor
+        noise = 8 * eps * (abs(fp) + abs(fm)) / (2 * h) + 1e-7 * abs(an)
+        worst = max(worst, abs(fd - an) / noise)
+    print(f"worst |FD - analytic| / noise floor over 64 directions: {worst:.3f}")
+    assert worst < 1.0
 
 
 def test_gradcheck_small():
@@ -79,8 +83,10 @@ def test_gradcheck_small():
     solver = cs.TriangularSolver(t(m.rowptr), t(m.colidx), t(m.val))
     val = t(m.val, True)
     b = t(np.random.default_rng(0).standard_normal((m.n, 3)), True)
+    # the backward accumulates with fp64 atomics: repeated backwards agree to
+    # rounding, not bit for bit (nondet_tol)
     assert torch.autograd.gradcheck(lambda vv, bb: cs.sptrsv(solver, vv, bb), (val, b), eps=1e-6,
-                                    atol=1e-7, rtol=1e-6)
+                                    atol=1e-7, rtol=1e-6, nondet_tol=1e-12)
 
 
 def test_module_with_parameter_trains():
@@ -96,5 +102,5 @@ def test_module_with_parameter_trains():
         loss = 0.5 * ((op(b) - target) ** 2).sum()
         loss.backward()
         opt.step()
-        losses.append(float(loss))
+        losses.append(float(loss.detach()))
     assert losses[-1] < losses[0]

@@ -43,13 +43,17 @@ def plain20k():
     return cs.generate("plain_20k", seed=0)
 
 
+SCHEDULES = ["level", "natural"]
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("alg", ["wrtfst", "twopart", "mix", "auto"])
 @pytest.mark.parametrize("on_device", [True, False])
-def test_plain_20k_fp64(plain20k, alg, on_device):
+def test_plain_20k_fp64(plain20k, alg, on_device, schedule):
     m = plain20k
     _, b = cs.get_x_b(m.n, m.n, m.rowptr, m.colidx, m.val)
     xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
-    s = solver_for(m, on_device=on_device, algorithm=alg)
+    s = solver_for(m, on_device=on_device, algorithm=alg, schedule=schedule)
     x = host(s.solve(dev(b)))
     s.status()
     assert rel_inf_err(x, xo) <= TOL64
@@ -71,24 +75,26 @@ def test_plain_20k_fp32_and_its_fp64_error(plain20k):
     assert err64 < 1e-4
 
 
+@pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("rows_per_thread", [1, 2, 4])
 @pytest.mark.parametrize("block", [64, 256, 512])
-def test_launch_shapes(plain20k, rows_per_thread, block):
+def test_launch_shapes(plain20k, rows_per_thread, block, schedule):
     m = plain20k
     b = cs.normal(m.n, seed=1)
     xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
-    s = solver_for(m)
+    s = solver_for(m, schedule=schedule)
     s.set_tuning(rows_per_thread, block, 0)
     x = host(s.solve(dev(b)))
     assert rel_inf_err(x, xo) <= TOL64
 
 
-def test_deterministic_and_schedules_agree(plain20k):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_deterministic_and_schedules_agree(plain20k, schedule):
     """Sums are taken in storage order whatever the arrival order: repeated solves
     and the write-first / two-phase schedules give identical bits."""
     m = plain20k
     b = dev(cs.normal(m.n, seed=2))
-    s = solver_for(m, algorithm="wrtfst")
+    s = solver_for(m, algorithm="wrtfst", schedule=schedule)
     x1, x2 = host(s.solve(b)), host(s.solve(b))
     s.set_algorithm("twopart")
     x3 = host(s.solve(b))
@@ -100,14 +106,15 @@ EDGE = ["single", "diagonal_only", "bidiagonal_chain", "stride64_chain", "dense_
         "ragged_33", "full_lower_64"]
 
 
+@pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("name", EDGE)
 @pytest.mark.parametrize("alg", ["wrtfst", "twopart", "mix"])
-def test_edge_cases_against_golden(golden, name, alg):
+def test_edge_cases_against_golden(golden, name, alg, schedule):
     rp, ci, v = (golden[f"edge_{name}_{k}"] for k in ("rowptr", "colidx", "val"))
     n = len(rp) - 1
     b1 = np.random.default_rng(11).standard_normal(n)
     b4 = np.random.default_rng(12).standard_normal((n, 4))
-    s = cs.TriangularSolver(dev(rp), dev(ci), dev(v), algorithm=alg)
+    s = cs.TriangularSolver(dev(rp), dev(ci), dev(v), algorithm=alg, schedule=schedule)
     s.set_mix_border(4)
     assert rel_inf_err(host(s.solve(dev(b1))), golden[f"edge_{name}_x1"]) <= TOL64
     assert rel_inf_err(host(s.solve(dev(b4))), golden[f"edge_{name}_x4"]) <= TOL64
@@ -116,15 +123,16 @@ def test_edge_cases_against_golden(golden, name, alg):
     s.status()
 
 
+@pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("nrhs", [1, 2, 3, 4, 8, 16, 32, 40])
-def test_multi_rhs_forward_adjoint_grad(nrhs):
+def test_multi_rhs_forward_adjoint_grad(nrhs, schedule):
     m = cs.generate(n=30_000, kmin=1, kmax=9, band=3000, seed=nrhs)
     b = np.random.default_rng(nrhs).standard_normal((m.n, nrhs))
     g = np.random.default_rng(nrhs + 100).standard_normal((m.n, nrhs))
     xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
     yo = oracle.solve_csr_transpose(m.rowptr, m.colidx, m.val, g)
     go = oracle.grad_val(m.rowptr, m.colidx, yo, xo)
-    s = solver_for(m)
+    s = solver_for(m, schedule=schedule)
     x = s.solve(dev(b))
     y, gv = s.solve_transpose_grad(dev(g), x)
     y2 = s.solve_transpose(dev(g))
@@ -137,43 +145,46 @@ def test_multi_rhs_forward_adjoint_grad(nrhs):
     assert rel_inf_err(host(gv2), go) <= TOL64
 
 
-def test_strided_rhs_layout():
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_strided_rhs_layout(schedule):
     """ld > nrhs: a column slice of a wider buffer."""
     m = cs.generate(n=5000, kmin=1, kmax=5, band=500, seed=8)
     wide = np.random.default_rng(0).standard_normal((m.n, 7))
     xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, wide[:, 2:5])
     bt = dev(wide)
     xt = torch.full_like(bt, 123.0)
-    s = solver_for(m)
+    s = solver_for(m, schedule=schedule)
     s.solve(bt[:, 2:5], xt[:, 2:5])
     out = host(xt)
     assert rel_inf_err(out[:, 2:5], xo) <= TOL64
     assert np.all(out[:, :2] == 123.0) and np.all(out[:, 5:] == 123.0)
 
 
-def test_wide_4m_full_size_fp64_and_fp32():
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_wide_4m_full_size_fp64_and_fp32(schedule):
     """The 4M-row workload at full size against the oracle (it finishes in well under a second)."""
     m = cs.generate("wide_4m", seed=0)
     _, b = cs.get_x_b(m.n, m.n, m.rowptr, m.colidx, m.val)
     xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
-    s = solver_for(m)
+    s = solver_for(m, schedule=schedule)
     x = host(s.solve(dev(b)))
     s.status()
     assert rel_inf_err(x, xo) <= TOL64
     v32 = m.val.astype(np.float32)
     _, b32 = cs.get_x_b(m.n, m.n, m.rowptr, m.colidx, v32)
     x32o = oracle.solve_csr_lower(m.rowptr, m.colidx, v32, b32)
-    s32 = solver_for(m, np.float32)
+    s32 = solver_for(m, np.float32, schedule=schedule)
     x32 = host(s32.solve(dev(b32)))
     assert rel_inf_err(x32, x32o) <= TOL32
     print(f"wide_4m FP32 vs FP64 oracle: {rel_inf_err(x32, xo):.3e}")
 
 
-def test_zipf_mix_path():
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_zipf_mix_path(schedule):
     m = cs.generate("zipf_1m", seed=0, n=200_000)
     b = cs.normal(m.n, seed=3)
     xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
-    s = solver_for(m, algorithm="mix")
+    s = solver_for(m, algorithm="mix", schedule=schedule)
     x = host(s.solve(dev(b)))
     s.status()
     info = s.info()
@@ -181,7 +192,8 @@ def test_zipf_mix_path():
     assert rel_inf_err(x, xo) <= TOL64
 
 
-def test_upper_csr_and_csc_paths():
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_upper_csr_and_csc_paths(schedule):
     """Upper-triangular CSR (backward substitution) and the CSC warp-per-column
     kernel, forward and transposed, against the oracle on the same matrix."""
     m = cs.generate(n=20_000, kmin=1, kmax=6, band=900, seed=5)
@@ -190,10 +202,10 @@ def test_upper_csr_and_csc_paths():
     xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)   # L x = b
     yo = oracle.solve_csr_transpose(m.rowptr, m.colidx, m.val, b)  # L^T y = b
     # CSC of L == CSR of U = L^T (diagonal first in each row)
-    up = cs.TriangularSolver(dev(cp), dev(ri), dev(cv), uplo="upper")
+    up = cs.TriangularSolver(dev(cp), dev(ri), dev(cv), uplo="upper", schedule=schedule)
     assert rel_inf_err(host(up.solve(dev(b))), yo) <= TOL64
     assert rel_inf_err(host(up.solve_transpose(dev(b))), xo) <= TOL64
-    csc = cs.TriangularSolver(dev(cp), dev(ri), dev(cv), fmt="csc")
+    csc = cs.TriangularSolver(dev(cp), dev(ri), dev(cv), fmt="csc", schedule=schedule)
     assert rel_inf_err(host(csc.solve(dev(b))), xo) <= TOL64
     assert rel_inf_err(host(csc.solve_transpose(dev(b))), yo) <= TOL64
     b4 = np.random.default_rng(4).standard_normal((m.n, 4))
@@ -250,11 +262,12 @@ def test_invalid_matrices_are_rejected():
         cs.TriangularSolver(rp, np.array([0, 0, 1], np.int32), np.array([1.0, 1.0, 0.0]))
 
 
-def test_timeout_is_reported_and_context_survives(plain20k):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_timeout_is_reported_and_context_survives(plain20k, schedule):
     """A row that never publishes (debug hook): its dependants' waits run out
     after 20 ms, the solve reports TIMEOUT, and the next solve is clean."""
     m = plain20k
-    s = solver_for(m)
+    s = solver_for(m, schedule=schedule)
     b = dev(cs.normal(m.n, seed=10))
     s.debug_stuck_row(5000, timeout_s=0.02)
     x = s.solve(b)
@@ -274,3 +287,11 @@ def test_hop_latency_probe_runs():
     lat_l2 = cs.hop_latency(n=20_000, stride=256)
     print(f"hop latency: in-warp {lat_warp:.0f} ns, cross-warp {lat_l2:.0f} ns")
     assert lat_warp > 0 and lat_l2 > 0
+
+
+def test_level_schedule_reports_levels(plain20k):
+    m = plain20k
+    s = solver_for(m)
+    info = s.info()
+    assert info["schedule"] == 1
+    assert info["levels"] == cs.matrix_layer(m.n, m.n, m.nnz, m.rowptr, m.colidx)[0]

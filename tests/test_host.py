@@ -173,6 +173,31 @@ def test_row_levels_histogram():
         assert level[i] == 1 + (level[deps].max() if len(deps) else 0)
 
 
+@pytest.mark.parametrize("upper", [False, True])
+def test_level_schedule_is_a_topological_level_order(upper):
+    from capellinisptrsv_gb300.solver import level_layout, level_schedule
+    m = cs.generate(n=4000, kmin=0, kmax=6, band=300, seed=6)
+    rp, ci, v = m.rowptr, m.colidx, m.val
+    if upper:  # the CSC of L is the CSR of U = L^T (diagonal first)
+        rp, ci, v = cs.matrix_transposition(m.n, m.n, m.nnz, m.rowptr, m.colidx, m.val)
+    levels, order, pos, start = level_schedule(m.n, rp, ci, upper)
+    assert levels == cs.matrix_layer(m.n, m.n, m.nnz, m.rowptr, m.colidx)[0]
+    assert sorted(order) == list(range(m.n)) and np.array_equal(pos[order], np.arange(m.n))
+    assert start[1] == 0 and start[levels + 1] == m.n
+    dep_ptr, dep_idx, dep_src, diag_src = level_layout(m.n, rp, ci, order, pos, upper)
+    for k in (0, 1, 777, m.n - 1):
+        i = order[k]
+        deps = dep_idx[dep_ptr[k]:dep_ptr[k + 1]]
+        assert np.all(deps < k) and np.all(np.diff(deps) > 0)         # dependencies come first
+        assert ci[diag_src[k]] == i
+        assert sorted(order[deps]) == sorted(ci[dep_src[dep_ptr[k]:dep_ptr[k + 1]]])
+        row = set(ci[rp[i]:rp[i + 1]]) - {i}
+        assert set(order[deps]) == row
+    # levels are contiguous blocks of positions
+    lev_of_pos = np.repeat(np.arange(1, levels + 1), np.diff(start[1:levels + 2]))
+    assert np.all(np.diff(lev_of_pos) >= 0)
+
+
 def _validate(rp, ci, fmt=N.FMT_CSR, uplo=N.LOWER):
     rp, ci = np.asarray(rp, np.int32), np.asarray(ci, np.int32)
     msg = C.create_string_buffer(256)
