@@ -92,6 +92,7 @@ _SIGS = {
     "capsp_debug_set_stuck_row": (I, [H, I, C.c_uint64]),
     "capsp_debug_trace": (I, [H, P]),
     "capsp_hop_latency": (I, [I, I, I, C.POINTER(C.c_float)]),
+    "capsp_csc_solve_noalloc_f64": (I, [P, P, P, I, I, P, P, P]),
     # reference-compatible drivers
     "spts_syncfree_cuda_csr_wrt_f64": (I, [P, P, P, I, I, I, DP, DP, DP]),
     "spts_syncfree_cuda_csr_wrt_f32": (I, [P, P, P, I, I, I, DP, DP, DP]),

@@ -1231,3 +1231,128 @@ extern "C" capsp_status_t capsp_hop_latency(int n, int stride, int dtype, float 
     *ns_per_hop = (float)(best * 1e6 / hops);
     return CAPSP_OK;
 }
+
+// ---------------------------------------------------------------------------
+// no-allocation column solve (static device scratch)
+// ---------------------------------------------------------------------------
+//
+// The scratch of the column-driven solve lives in one file-scope device array
+// instead of handle allocations: a 256-byte header (ticket at byte 0, the
+// four-int error word at byte 16, the first malformed column at byte 32),
+// then 1/diag and left_sum (double[kNoallocMaxN] each) and the in-degree and
+// arrival counters (int[kNoallocMaxN] each): 24 bytes per row, 1.5 MiB in all.
+// Every part that must start at zero (ticket, error word, left_sum, both
+// counter arrays) or at "no bad row" (0x7F7F7F7F) is reset on the stream at
+// the start of every call, so the caller prepares nothing.
+
+namespace {
+
+constexpr int kNoallocMaxN = 65536;
+constexpr size_t kNoallocHeader = 256;
+constexpr size_t kNoallocInv = kNoallocHeader;
+constexpr size_t kNoallocLeft = kNoallocInv + sizeof(double) * kNoallocMaxN;
+constexpr size_t kNoallocIndeg = kNoallocLeft + sizeof(double) * kNoallocMaxN;
+constexpr size_t kNoallocArrived = kNoallocIndeg + sizeof(int) * kNoallocMaxN;
+constexpr size_t kNoallocBytes = kNoallocArrived + sizeof(int) * kNoallocMaxN;
+constexpr int kNoallocMaxDevices = 64;
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_base[kNoallocMaxDevices] = {};
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+extern "C" capsp_status_t capsp_csc_solve_noalloc_f64(const int *colptr, const int *rowidx,
+                                                      const double *val, int n, int nnz,
+                                                      const double *b, double *x, void *stream)
+{
+    if (!colptr || !rowidx || !val || !b || !x)
+        return fail(CAPSP_ERR_INVALID, "all array pointers must be non-NULL");
+    if (n < 1 || nnz < n)
+        return fail(CAPSP_ERR_INVALID, "need n >= 1 and nnz >= n (got n=%d nnz=%d)", n, nnz);
+    if (n > kNoallocMaxN)
+        return fail(CAPSP_ERR_INVALID,
+                    "n=%d exceeds the static scratch of capsp_csc_solve_noalloc_f64 (at most %d rows)", n,
+                    kNoallocMaxN);
+    if ((const void *)b == (const void *)x)
+        return fail(CAPSP_ERR_INVALID, "b and x must not alias");
+    // one call at a time in this process: every call uses the same scratch
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    int dev = 0, sms = 0;
+    CAPSP_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoallocMaxDevices)
+        return fail(CAPSP_ERR_UNSUPPORTED, "device ordinal %d is beyond %d", dev, kNoallocMaxDevices);
+    if (!g_noalloc_base[dev]) {
+        // first call on this device: resolve the scratch address with the device current
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(CAPSP_ERR_CUDA, "cudaGetSymbolAddress of the static scratch failed: %s",
+                        cudaGetErrorString(e));
+        g_noalloc_base[dev] = p;
+    }
+    CAPSP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    unsigned char *base = static_cast<unsigned char *>(g_noalloc_base[dev]);
+    unsigned *ticket = reinterpret_cast<unsigned *>(base);
+    int *err = reinterpret_cast<int *>(base + 16);
+    int *bad = reinterpret_cast<int *>(base + 32);
+    double *inv = reinterpret_cast<double *>(base + kNoallocInv);
+    double *left = reinterpret_cast<double *>(base + kNoallocLeft);
+    int *indeg = reinterpret_cast<int *>(base + kNoallocIndeg);
+    int *arrived = reinterpret_cast<int *>(base + kNoallocArrived);
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t nn = (size_t)n;
+
+    // structure first: a malformed column must not reach the solve
+    CAPSP_CUDA(cudaMemsetAsync(base, 0, 32, st));        // ticket + error word
+    CAPSP_CUDA(cudaMemsetAsync(err + 3, 0x7F, sizeof(int), st));
+    CAPSP_CUDA(cudaMemsetAsync(bad, 0x7F, sizeof(int), st));
+    CAPSP_CUDA(launch_validate(colptr, rowidx, n, nnz, 0, bad, st));
+    int h_bad = 0;
+    CAPSP_CUDA(cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CAPSP_CUDA(cudaStreamSynchronize(st));
+    if (h_bad < n)
+        return fail(CAPSP_ERR_INVALID, "column %d is malformed (lower CSC needs the diagonal first, "
+                                       "rows ascending and below it)", h_bad);
+
+    CAPSP_CUDA(cudaMemsetAsync(left, 0, sizeof(double) * nn, st));
+    CAPSP_CUDA(cudaMemsetAsync(indeg, 0, sizeof(int) * nn, st));
+    CAPSP_CUDA(cudaMemsetAsync(arrived, 0, sizeof(int) * nn, st));
+    CAPSP_CUDA(launch_inv_diag<double>(colptr, val, inv, n, 0, err + 3, st));
+    CAPSP_CUDA(launch_histogram(rowidx, nnz, indeg, st));
+    ColArgs<double> a;
+    a.ptr = colptr;
+    a.idx = rowidx;
+    a.val = val;
+    a.inv_diag = inv;
+    a.indeg = indeg;
+    a.arrived = arrived;
+    a.left_sum = left;
+    a.lsld = 1;
+    a.b = b;
+    a.x = x;
+    a.ld = 1;
+    a.n = n;
+    a.nrhs = 1;
+    a.backward = 0;
+    a.xf = nullptr;
+    a.grad_val = nullptr;
+    a.grad_accumulate = 0;
+    a.ticket = ticket;
+    a.err = err;
+    a.wait = WaitCfg{10000000000ull, 1u << 30, 256u};
+    a.stuck_row = -1;
+    CAPSP_CUDA(launch_col_solve<double>(a, 256, 0, sms, st));
+    int h_err[4] = {0, 0, 0, 0};
+    CAPSP_CUDA(cudaMemcpyAsync(h_err, err, sizeof(h_err), cudaMemcpyDeviceToHost, st));
+    CAPSP_CUDA(cudaStreamSynchronize(st));
+    if (h_err[3] < n)
+        return fail(CAPSP_ERR_INVALID, "column %d has a zero or non-finite diagonal", h_err[3]);
+    if (h_err[kErrStatus] == kStatusTimeout)
+        return fail(CAPSP_ERR_TIMEOUT, "column %d gave up waiting (dependency %d)", h_err[kErrRow],
+                    h_err[kErrWaitedOn]);
+    if (h_err[kErrStatus] != 0)
+        return fail(CAPSP_ERR_CUDA, "device status %d", h_err[kErrStatus]);
+    return CAPSP_OK;
+}

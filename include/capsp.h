@@ -264,6 +264,21 @@ capsp_status_t capsp_debug_set_stuck_row(capsp_handle_t h, int row, uint64_t tim
  * number of hops.  Allocates and frees its own matrix. */
 capsp_status_t capsp_hop_latency(int n, int stride, int dtype, float *ns_per_hop);
 
+/* No counterpart in the reference.  Lower-triangular CSC solve Lx = b in FP64
+ * (the column-driven solve, one right-hand side) that allocates nothing: its
+ * scratch (1/diag, left_sum, in-degree and arrival counters, ticket, error
+ * word) is one static device array sized for at most 65,536 rows; a larger n
+ * is rejected with CAPSP_ERR_INVALID.  All pointers are device pointers;
+ * colptr/rowidx must hold the diagonal first in each column (checked on the
+ * device before the solve).  The call resets every scratch part that must
+ * start at zero itself, then synchronises `stream` and returns the solve's
+ * status.  The first call on a device resolves the scratch address
+ * (cudaGetSymbolAddress, with that device current) and must come before any
+ * stream capture.  All calls share the scratch, so overlapping calls would
+ * race on it: a process-wide lock serialises them. */
+capsp_status_t capsp_csc_solve_noalloc_f64(const int *colptr, const int *rowidx, const double *val,
+                                           int n, int nnz, const double *b, double *x, void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* 2. Reference-compatible drivers (exact reference argument lists)          */
 /*    Each allocates device memory, builds b = L*ones (get_x_b), runs        */
