@@ -30,12 +30,16 @@
 //   * Value-as-flag readiness (capsp_device.cuh): no flag array, no fence.
 //   * Dependencies inside the warp's own chunk are read from a per-warp
 //     shared-memory mirror of the chunk's values instead of from L2.
-//   * Polling: the first sweep polls every dependency; afterwards only the
-//     newest pending one is polled until it lands, then the rest are swept.
+//   * Polling: a fresh batch of dependencies is swept once; afterwards each
+//     lane probes only the dependency that blocks its in-order fold, and the
+//     next round's probe is issued before the current round folds and
+//     publishes, so the poll's round trip overlaps that work.
 //   * Partial sums are accumulated in storage order whatever the arrival
 //     order, so repeated solves and the WRTFST / TWOPART schedules are
 //     bit-identical.
-//   * 1/diag is precomputed at analysis; x = (b - sum) * (1/diag).
+//   * 1/diag is precomputed at analysis; x = (b - sum) * (1/diag).  The
+//     level schedule pre-scales the values instead (x = b/d + sum (-v/d) x_j),
+//     so a single FMA follows the last dependency.
 //   * Multi-RHS: G = next_pow2(nrhs) lanes share a row, one right-hand side
 //     each; every (row, rhs) element is published and polled independently.
 //   * Every wait is bounded (Spin); a lane that gives up publishes a quiet
@@ -190,7 +194,9 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
     int c[kBatch];                    // dependency index (position, or row in natural order)
     unsigned pend = 0, ext = 0, need = 0;
     int nacc = 0, cnt = 0;
+    bool sweep_next = false;          // a fresh batch is swept once, then probed
     auto load_batch = [&]() {
+        sweep_next = true;
         cnt = min(kBatch, e - j0);
         pend = ext = need = 0;
         nacc = 0;
@@ -215,9 +221,12 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
             }
         }
     };
-    // fold the contributions of the ready prefix [nacc, first pending)
+    // fold the contributions of the ready prefix [nacc, first pending).  Not
+    // unrolled: an unrolled copy issues predicated-off FMAs, and every warp
+    // FP64 instruction holds the sub-partition's FP64 pipe for ~64 cycles.
     auto fold = [&]() {
         const int lim = pend ? __ffs(pend) - 1 : cnt;
+#pragma unroll 1
         for (int t = nacc; t < lim; ++t)
             acc = fma(sl.v[t * 32 + lane], VB::from(sl.w[t * 32 + lane]), acc);
         nacc = lim;
@@ -225,7 +234,9 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
     bool done = !mine, published = !mine;
     if (mine && j0 < e)
         load_batch();
-    bool probe_only = false, aborted = false;
+    bool aborted = false;
+    U u_next = VB::kPending;          // probe issued at the end of the previous round
+    unsigned top_next = 0u;           // ... and the slot it polls
     unsigned long long t_ready = 0;
     Spin sp;
     int waited = 0;
@@ -235,29 +246,32 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
         t_first = global_timer_ns();
     for (;;) {
         // ---- A: polls of dependencies before the chunk ---------------------
-        // The first round polls every outstanding dependency; afterwards each
-        // lane polls only its newest outstanding one until it lands, then
-        // sweeps the rest.  The two-phase schedule instead walks each lane's
-        // outside dependencies one at a time, oldest first.
+        // A fresh batch is swept once: every outstanding dependency polled,
+        // all loads in flight together.  After that each lane probes one
+        // dependency per round, its first pending one in storage order (the
+        // one that blocks the in-order fold), so by the time the last one
+        // lands everything before it has been folded.  The two-phase
+        // schedule never sweeps.  Each round issues the next round's probe
+        // at its end, so the poll travels while this round folds, publishes
+        // and backs off.
         bool changed = first;
         first = false;
         const unsigned ext_pend = done ? 0u : (pend & ext);
-        unsigned top = 0u;
-        if (TWO)
-            top = ext_pend & (0u - ext_pend);  // oldest outside dependency first
-        else if (ext_pend)
-            top = (!LEVEL && a.upper) ? (ext_pend & (0u - ext_pend)) : (1u << (31 - __clz(ext_pend)));
-        const bool sweep = !TWO && ext_pend != 0u && !probe_only;
+        const unsigned top = ext_pend & (0u - ext_pend);
+        const bool sweep = !TWO && ext_pend != 0u && sweep_next;
+        sweep_next = false;
         if (!__any_sync(kFullMask, sweep)) {
-            // probe round (warp-uniform): one branch-free load per lane, the
-            // lane's newest (oldest for TWO) outside dependency; lanes with
-            // nothing outstanding read their own slot
-            const U *addr = pub + (size_t)pslot * (size_t)pld + g;
+            // probe round (warp-uniform): the value polled at the end of the
+            // previous round when it was for this slot, else a fresh load
+            U u0 = u_next;
+            if (top != 0u && top != top_next) {
+                const U *addr = pub;
 #pragma unroll
-            for (int t = 0; t < kBatch; ++t)
-                if ((top >> t) & 1u)
-                    addr = pub + (size_t)c[t] * (size_t)pld + g;
-            const U u0 = mine ? ld_relaxed(addr, pol.keep) : VB::kPending;
+                for (int t = 0; t < kBatch; ++t)
+                    if ((top >> t) & 1u)
+                        addr = pub + (size_t)c[t] * (size_t)pld + g;
+                u0 = ld_relaxed(addr, pol.keep);
+            }
             if (top) {
                 if (u0 != VB::kPending) {
 #pragma unroll
@@ -266,7 +280,6 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
                             sl.w[t * 32 + lane] = u0;
                     pend &= ~top;
                     changed = true;
-                    probe_only = false;  // the newest landed: sweep the others next
                     if (a.trace != nullptr && pend == 0 && j0 + kBatch >= e)
                         t_ready = global_timer_ns();  // last dependency value received
                 } else {
@@ -278,22 +291,19 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
                     waited = w;
                 }
             }
-            if ((pend & ext) == 0u)
-                probe_only = false;
         } else if (ext_pend) {
             // sweep round: every outstanding outside dependency, all loads in
             // flight together before any result is consumed (in-order issue
             // would otherwise stall on the first result)
-            const unsigned sel = probe_only ? top : ext_pend;
             U u[kBatch];
 #pragma unroll
             for (int t = 0; t < kBatch; ++t)
-                u[t] = ((sel >> t) & 1u) ? ld_relaxed(pub + (size_t)c[t] * (size_t)pld + g, pol.keep)
-                                         : VB::kPending;
+                u[t] = ((ext_pend >> t) & 1u) ? ld_relaxed(pub + (size_t)c[t] * (size_t)pld + g, pol.keep)
+                                              : VB::kPending;
             unsigned got = 0;
 #pragma unroll
             for (int t = 0; t < kBatch; ++t) {
-                if ((sel >> t) & 1u) {
+                if ((ext_pend >> t) & 1u) {
                     if (u[t] != VB::kPending) {
                         sl.w[t * 32 + lane] = u[t];
                         got |= 1u << t;
@@ -303,10 +313,24 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
                 }
             }
             pend &= ~got;
-            probe_only = (pend & ext) != 0 && !(got & top);
             changed = changed || got != 0;
             if (a.trace != nullptr && got != 0 && pend == 0 && j0 + kBatch >= e)
                 t_ready = global_timer_ns();  // last dependency value received
+        }
+        {
+            // next round's probe (B and C leave the outside part of pend alone;
+            // a batch loaded in B is swept instead)
+            const unsigned np = done ? 0u : (pend & ext);
+            top_next = np & (0u - np);
+            u_next = VB::kPending;
+            if (top_next != 0u) {
+                const U *addr = pub;
+#pragma unroll
+                for (int t = 0; t < kBatch; ++t)
+                    if ((top_next >> t) & 1u)
+                        addr = pub + (size_t)c[t] * (size_t)pld + g;
+                u_next = ld_relaxed(addr, pol.keep);
+            }
         }
         // a lane whose current batch is complete but not yet folded also needs B
         const bool progress = __any_sync(kFullMask, changed || (!done && pend == 0u));
@@ -335,7 +359,6 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
                         j0 += kBatch;
                         if (j0 < e) {
                             load_batch();  // a row with more than kBatch dependencies
-                            probe_only = false;
                             moved = true;
                         } else {
                             if (a.trace != nullptr && t_ready == 0)
@@ -463,6 +486,7 @@ __device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const
             probe_only = pend != 0 && !(got & top);
             progress = got != 0;
             if (pend == 0) {
+#pragma unroll 1
                 for (int t = 0; t < cnt; ++t)
                     acc = fma(sl.v[t * 32 + lane], VB::from(sl.w[t * 32 + lane]), acc);
                 j0 += NS * kBatch;
