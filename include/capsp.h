@@ -265,10 +265,15 @@ capsp_status_t capsp_debug_set_stuck_row(capsp_handle_t h, int row, uint64_t tim
 capsp_status_t capsp_hop_latency(int n, int stride, int dtype, float *ns_per_hop);
 
 /* No counterpart in the reference.  Lower-triangular CSC solve Lx = b in FP64
- * (the column-driven solve, one right-hand side) that allocates nothing: its
- * scratch (1/diag, left_sum, in-degree and arrival counters, ticket, error
- * word) is one static device array sized for at most 65,536 rows; a larger n
- * is rejected with CAPSP_ERR_INVALID.  All pointers are device pointers;
+ * (the column-driven solve, one right-hand side) that allocates nothing, for
+ * callers that must not call cudaMalloc: code whose host framework owns all
+ * device memory through its own pool (so a private allocation could fail or
+ * break its budget), and code on a latency-critical path, where cudaMalloc /
+ * cudaFree can synchronise the device and stall other streams.  Its scratch
+ * (1/diag, left_sum, in-degree and arrival counters, ticket, error word) is
+ * one static device array of 1.5 MiB, sized for at most 65,536 rows, that
+ * every GPU which loads the library holds until the process exits; a larger
+ * n is rejected with CAPSP_ERR_INVALID.  All pointers are device pointers;
  * colptr/rowidx must hold the diagonal first in each column (checked on the
  * device before the solve).  The call resets every scratch part that must
  * start at zero itself, then synchronises `stream` and returns the solve's

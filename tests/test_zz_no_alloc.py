@@ -1,7 +1,11 @@
 """capsp_csc_solve_noalloc_f64: the column-driven CSC solve on static device
-scratch, called through the C ABI and compared with the handle-based CSC solve
-of the same matrix (and with the oracle) on two consecutive calls.  The file is
-collected last so that it also runs after every other GPU test."""
+scratch, for callers that may not allocate device memory (a host framework
+that owns all of it through its own pool, or a latency-critical path where
+cudaMalloc would synchronise the device).  It is called through the C ABI and
+compared with the handle-based CSC solve of the same matrix (and with the
+oracle) on two consecutive calls, which also shows that the scratch left by
+one call does not leak into the next.  The file is collected last so that it
+also runs after every other GPU test."""
 from __future__ import annotations
 
 import ctypes as C
