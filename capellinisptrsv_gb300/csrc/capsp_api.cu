@@ -65,6 +65,7 @@ struct Tuning {
     int block;  // threads per block
     int bps;    // blocks per SM (0: occupancy maximum)
     int border; // mix border
+    bool dflt;  // the handle's defaults (no explicit or autotuned choice)
 };
 
 struct MixTable {
@@ -120,6 +121,9 @@ struct capsp_handle_s {
     // warps per SM; more resident warps only add pollers
     Tuning tune = {kRowWrtFst, 1, 256, 1, 10};
     bool tune_explicit = false;
+    // levels narrower than ~4k rows: two resident warps per SM for the row
+    // path by default (more rows in flight than a few levels only add pollers)
+    bool narrow_levels = false;
     std::map<int, Tuning> tuned;
     WaitCfg wait = {10000000000ull, 1u << 30, 256u};
     int stuck_row = -1;
@@ -270,6 +274,7 @@ static capsp_status_t build_level(capsp_handle_t h)
     for (int k = 0; k <= n; ++k)
         h->h_lcum[k] = lptr[k] + k;
     h->levels = levels;
+    h->narrow_levels = (long long)n < 4096LL * (long long)levels;
     h->level_built = true;
     int *d_bad = nullptr;
     CAPSP_CUDA(cudaMalloc(&d_bad, sizeof(int)));
@@ -633,6 +638,12 @@ static capsp_status_t ensure_column_scratch(capsp_handle_t h, int nrhs)
     return CAPSP_OK;
 }
 
+// threads per block of a row-path launch
+static int row_block(capsp_handle_t h, const Tuning &tn)
+{
+    return (tn.dflt && h->narrow_levels && h->sched == CAPSP_SCHED_LEVEL) ? 64 : tn.block;
+}
+
 static Tuning current_tuning(capsp_handle_t h, int nrhs)
 {
     auto it = h->tuned.find(nrhs);
@@ -640,6 +651,7 @@ static Tuning current_tuning(capsp_handle_t h, int nrhs)
         return it->second;
     Tuning t = h->tune;
     t.border = h->border;
+    t.dflt = !h->tune_explicit;
     switch (h->alg) {
     case CAPSP_ALG_TWOPART: t.kind = kRowTwoPart; break;
     case CAPSP_ALG_MIX: t.kind = kRowMix; break;
@@ -722,7 +734,7 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs,
         const bool prof = h->profiling && r0 == 0;
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k0, st));
-        CAPSP_CUDA(launch_row_solve<T>(a, kind, tn.R, tn.block, tn.bps, h->num_sms, st));
+        CAPSP_CUDA(launch_row_solve<T>(a, kind, tn.R, row_block(h, tn), tn.bps, h->num_sms, st));
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k1, st));
     }
@@ -1137,7 +1149,7 @@ extern "C" capsp_status_t capsp_get_info(capsp_handle_t h, capsp_info_t *info)
     info->num_sms = h->num_sms;
     Tuning tn = current_tuning(h, 1);
     info->rows_per_thread = tn.R;
-    info->block_threads = tn.block;
+    info->block_threads = h->format == CAPSP_FMT_CSR ? row_block(h, tn) : tn.block;
     info->blocks_per_sm = tn.bps;
     info->schedule = h->sched;
     info->levels = h->levels;
