@@ -112,6 +112,8 @@ struct capsp_handle_s {
     int *d_err = nullptr;          // [4]
     int *d_indeg = nullptr;
     int *d_arrived = nullptr;
+    int *d_corder[2] = {nullptr, nullptr};  // column-path visiting order: [forward, backward]
+    bool col_narrow[2] = {false, false};     // ... and whether its levels are narrower than ~4k
     void *d_left = nullptr;
     int left_cap = 0;  // right-hand sides the left_sum scratch holds
     std::map<int, MixTable> mix;
@@ -170,6 +172,8 @@ static void free_handle(capsp_handle_t h)
     cudaFree(h->d_ticket);
     cudaFree(h->d_indeg);
     cudaFree(h->d_arrived);
+    cudaFree(h->d_corder[0]);
+    cudaFree(h->d_corder[1]);
     cudaFree(h->d_left);
     cudaFree(h->d_stage);
     cudaFree(h->d_perm);
@@ -638,6 +642,57 @@ static capsp_status_t ensure_column_scratch(capsp_handle_t h, int nrhs)
     return CAPSP_OK;
 }
 
+// Visiting order of the column-driven solve: columns stable-sorted by their
+// level in the column DAG (a column's level is one more than the deepest
+// column that scatters into it).  Warps then take columns that become ready
+// together instead of a window of consecutive indices that holds only a few
+// columns of the current level.  Every producer of a column comes before it,
+// so ticket order keeps forward progress independent of block scheduling.
+// Forward: columns ascend and scatter into rows below the diagonal; backward:
+// columns descend and scatter into smaller indices (the transpose solve on
+// the CSR arrays of a lower-triangular matrix).
+static capsp_status_t ensure_column_order(capsp_handle_t h, int backward)
+{
+    if (h->d_corder[backward])
+        return CAPSP_OK;
+    const int n = h->n, nnz = h->nnz;
+    std::vector<int> idx((size_t)nnz);
+    CAPSP_CUDA(cudaMemcpy(idx.data(), h->d_idx, sizeof(int) * (size_t)nnz, cudaMemcpyDeviceToHost));
+    const int *ptr = h->h_ptr.data();
+    std::vector<int> lev((size_t)n, 0);
+    int deepest = 0;
+    for (int s = 0; s < n; ++s) {
+        const int j = backward ? n - 1 - s : s;
+        const int next = lev[j] + 1;
+        if (lev[j] > deepest)
+            deepest = lev[j];
+        for (int k = ptr[j]; k < ptr[j + 1]; ++k) {
+            const int r = idx[k];
+            if (r != j && lev[r] < next)
+                lev[r] = next;
+        }
+    }
+    std::vector<int> start((size_t)deepest + 2, 0), order((size_t)n);
+    for (int j = 0; j < n; ++j)
+        ++start[(size_t)lev[j] + 1];
+    for (int l = 0; l <= deepest; ++l)
+        start[(size_t)l + 1] += start[(size_t)l];
+    for (int s = 0; s < n; ++s) {
+        const int j = backward ? n - 1 - s : s;
+        order[(size_t)start[(size_t)lev[j]]++] = j;
+    }
+    int *d = nullptr;
+    CAPSP_CUDA(cudaMalloc(&d, sizeof(int) * (size_t)n));
+    const cudaError_t e = cudaMemcpy(d, order.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return fail(CAPSP_ERR_CUDA, "column order upload failed: %s", cudaGetErrorString(e));
+    }
+    h->d_corder[backward] = d;
+    h->col_narrow[backward] = (long long)n < 4096LL * (long long)(deepest + 1);
+    return CAPSP_OK;
+}
+
 // threads per block of a row-path launch
 static int row_block(capsp_handle_t h, const Tuning &tn)
 {
@@ -747,6 +802,7 @@ static capsp_status_t enqueue_cols(capsp_handle_t h, const T *b, T *x, int nrhs,
                                    cudaStream_t st)
 {
     CAPSP_TRY(ensure_column_scratch(h, nrhs));
+    CAPSP_TRY(ensure_column_order(h, backward));
     for (int r0 = 0; r0 < nrhs; r0 += 32) {
         const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
         CAPSP_CUDA(cudaMemsetAsync(h->d_arrived, 0, sizeof(int) * (size_t)h->n, st));
@@ -760,6 +816,7 @@ static capsp_status_t enqueue_cols(capsp_handle_t h, const T *b, T *x, int nrhs,
         a.val = (const T *)h->d_val;
         a.inv_diag = (const T *)h->d_inv;
         a.indeg = h->d_indeg;
+        a.order = h->d_corder[backward];
         a.arrived = h->d_arrived;
         a.left_sum = (T *)h->d_left;
         a.lsld = nb;
@@ -779,7 +836,12 @@ static capsp_status_t enqueue_cols(capsp_handle_t h, const T *b, T *x, int nrhs,
         const bool prof = h->profiling && r0 == 0;
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k0, st));
-        CAPSP_CUDA(launch_col_solve<T>(a, tn.block, tn.bps, h->num_sms, st));
+        // default launch shape of the column path (measured on GB300): a warp
+        // holds one column, so wide levels want every warp an SM can hold,
+        // narrow ones two 256-thread blocks per SM
+        const int cblock = tn.dflt ? 256 : tn.block;
+        const int cbps = tn.dflt ? (h->col_narrow[backward] ? 2 : 0) : tn.bps;
+        CAPSP_CUDA(launch_col_solve<T>(a, cblock, cbps, h->num_sms, st));
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k1, st));
     }
@@ -1339,6 +1401,7 @@ extern "C" capsp_status_t capsp_csc_solve_noalloc_f64(const int *colptr, const i
     a.val = val;
     a.inv_diag = inv;
     a.indeg = indeg;
+    a.order = nullptr;
     a.arrived = arrived;
     a.left_sum = left;
     a.lsld = 1;

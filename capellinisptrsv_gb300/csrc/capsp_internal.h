@@ -57,6 +57,7 @@ struct ColArgs {
     const T *val;
     const T *inv_diag;
     const int *indeg;  // entries targeting each row, diagonal included
+    const int *order;  // visiting order of the columns (nullptr: index order)
     int *arrived;      // zeroed before the launch
     T *left_sum;       // zeroed before the launch, element (i, r) at i*lsld + r
     long long lsld;

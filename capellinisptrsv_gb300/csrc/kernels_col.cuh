@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(512) col_solve_kernel(const ColArgs<T> a)
         stop = __shfl_sync(kFullMask, stop, 0);
         if (stop || tk >= (unsigned)a.n)
             break;
-        const int j = a.backward ? a.n - 1 - (int)tk : (int)tk;
+        const int j = a.order != nullptr ? __ldg(a.order + tk) : (a.backward ? a.n - 1 - (int)tk : (int)tk);
         const int s0 = __ldg(a.ptr + j), e0 = __ldg(a.ptr + j + 1);
         const int s = a.backward ? s0 : s0 + 1;
         const int e = a.backward ? e0 - 1 : e0;
