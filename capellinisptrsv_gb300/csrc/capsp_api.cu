@@ -693,10 +693,29 @@ static capsp_status_t ensure_column_order(capsp_handle_t h, int backward)
     return CAPSP_OK;
 }
 
-// threads per block of a row-path launch
-static int row_block(capsp_handle_t h, const Tuning &tn)
+// Launch shape of a row-path launch with nrhs right-hand sides.  Defaults
+// measured on GB300: with one lane per row (32 rows per warp) eight resident
+// warps per SM suit wide levels and two suit narrow ones (more rows in flight
+// than a few levels only add pollers); with G >= 4 lanes per row a warp holds
+// few rows, so every warp the SM can hold in 128-thread blocks pays off.
+static void row_shape(capsp_handle_t h, const Tuning &tn, int nrhs, int *block, int *bps)
 {
-    return (tn.dflt && h->narrow_levels && h->sched == CAPSP_SCHED_LEVEL) ? 64 : tn.block;
+    *block = tn.block;
+    *bps = tn.bps;
+    if (!tn.dflt)
+        return;
+    const int g = lanes_for_rhs(nrhs);
+    const bool narrow = h->narrow_levels && h->sched == CAPSP_SCHED_LEVEL;
+    if (g == 1) {
+        *block = narrow ? 64 : 256;
+        *bps = 1;
+    } else if (g == 2) {
+        *block = 256;
+        *bps = narrow ? 1 : 0;
+    } else {
+        *block = 128;
+        *bps = 0;
+    }
 }
 
 static Tuning current_tuning(capsp_handle_t h, int nrhs)
@@ -789,7 +808,9 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs,
         const bool prof = h->profiling && r0 == 0;
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k0, st));
-        CAPSP_CUDA(launch_row_solve<T>(a, kind, tn.R, row_block(h, tn), tn.bps, h->num_sms, st));
+        int blk = 0, bps = 0;
+        row_shape(h, tn, nb, &blk, &bps);
+        CAPSP_CUDA(launch_row_solve<T>(a, kind, tn.R, blk, bps, h->num_sms, st));
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k1, st));
     }
@@ -1032,12 +1053,16 @@ extern "C" capsp_status_t capsp_autotune(capsp_handle_t h, const void *b, void *
     cudaStream_t st = (cudaStream_t)stream;
     std::vector<Tuning> cands;
     const bool row_path = h->format == CAPSP_FMT_CSR;
-    const int blocks[3] = {128, 256, 512};
+    const int blocks[3] = {64, 128, 256};
     if (row_path) {
-        const int rs[3] = {1, 2, 4};
+        const int rs[2] = {1, 2};
         const bool allow_thread = h->alg == CAPSP_ALG_AUTO || h->alg == CAPSP_ALG_WRTFST;
         const bool allow_mix = h->alg == CAPSP_ALG_AUTO || h->alg == CAPSP_ALG_MIX;
-        const int bpss[2] = {0, 2};
+        const int bpss[3] = {1, 2, 0};
+        if (allow_thread) {
+            // the default launch shape first: the search never ends worse
+            cands.push_back({kRowWrtFst, 1, 256, 1, h->border, true});
+        }
         if (allow_thread)
             for (int bl : blocks)
                 for (int r : rs)
@@ -1055,8 +1080,10 @@ extern "C" capsp_status_t capsp_autotune(capsp_handle_t h, const void *b, void *
                     cands.push_back({kRowMix, 1, bl, 0, bo});
         }
     } else {
+        cands.push_back({kRowWrtFst, 1, 256, 0, h->border, true});  // the default shape
         for (int bl : blocks)
-            cands.push_back({kRowWrtFst, 1, bl, 0, h->border});
+            for (int bp : {0, 2})
+                cands.push_back({kRowWrtFst, 1, bl, bp, h->border});
     }
     cudaEvent_t e0, e1;
     CAPSP_CUDA(cudaEventCreate(&e0));
@@ -1211,8 +1238,11 @@ extern "C" capsp_status_t capsp_get_info(capsp_handle_t h, capsp_info_t *info)
     info->num_sms = h->num_sms;
     Tuning tn = current_tuning(h, 1);
     info->rows_per_thread = tn.R;
-    info->block_threads = h->format == CAPSP_FMT_CSR ? row_block(h, tn) : tn.block;
-    info->blocks_per_sm = tn.bps;
+    int blk = tn.block, bps = tn.bps;
+    if (h->format == CAPSP_FMT_CSR)
+        row_shape(h, tn, 1, &blk, &bps);
+    info->block_threads = blk;
+    info->blocks_per_sm = bps;
     info->schedule = h->sched;
     info->levels = h->levels;
     if (h->format == CAPSP_FMT_CSC) {
