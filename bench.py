@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-vendor", action="store_true", help="skip the cuSPARSE SpSV side-by-side")
     return ap.parse_args()
 
 
@@ -349,6 +350,7 @@ def run_native(args):
         e2e = None
         if not args.no_e2e:
             e2e = e2e_measure(cs, m, val, b, args, flops)
+        vendor = None if args.no_vendor else vendor_measure(m, rp_d, ci_d, val_d, b_d, args, flops, kms)
         cpu = None
         if not args.no_cpu_baseline:
             run, kind = cpu_arm_runner(m, val)
@@ -378,6 +380,7 @@ def run_native(args):
                          "algorithmic_bytes_per_launch": alg_bytes},
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "cusparse_spsv": vendor,
             "gpu_launches": 2 * args.steps,
             "gflops_2nnz": world * 2.0 * m.nnz / (ms * 1e-3) / 1e9,
             "gbs_algorithmic": alg_bytes / (ms * 1e-3) / 1e9,
@@ -389,6 +392,35 @@ def run_native(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def vendor_measure(m, rp_d, ci_d, val_d, b_d, args, flops, capsp_kernel_ms):
+    """cuSPARSE SpSV on the same device arrays: measured side-by-side, not a baseline of the metric."""
+    import ctypes as C
+    import torch
+    lib_path = ROOT / "capellinisptrsv_gb300" / "_build" / "libcapsp_vendor.so"
+    if not lib_path.exists():
+        return {"unavailable": "libcapsp_vendor.so was not built"}
+    lib = C.CDLL(str(lib_path))
+    lib.capsp_vendor_spsv.restype = C.c_int
+    lib.capsp_vendor_spsv.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                      C.c_void_p, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    lib.capsp_vendor_last_error.restype = C.c_char_p
+    x = torch.empty_like(b_d)
+    an, so = C.c_float(), C.c_float()
+    reps = max(3, min(args.steps, 20))
+    torch.cuda.synchronize()
+    rc = lib.capsp_vendor_spsv(m.n, m.nnz, rp_d.data_ptr(), ci_d.data_ptr(), val_d.data_ptr(),
+                               0 if args.dtype == "f64" else 1, b_d.data_ptr(), x.data_ptr(), reps,
+                               C.byref(an), C.byref(so))
+    if rc != 0:
+        return {"unavailable": lib.capsp_vendor_last_error().decode()}
+    err = float((x.double() - 1.0).abs().max())
+    return {"solve_ms": so.value, "value": flops / (so.value * 1e-3) / 1e9, "unit": "GFLOP/s",
+            "analysis_ms": an.value, "solves_timed": reps, "max_abs_x_minus_ones": err,
+            "capsp_kernel_speedup": so.value / capsp_kernel_ms,
+            "what": "cusparseSpSV_solve (CUSPARSE_SPSV_ALG_DEFAULT, lower, non-unit) on the same device CSR "
+                    "arrays, back-to-back solves after analysis; CUDA events"}
 
 
 def e2e_measure(cs, m, val, b, args, flops):

@@ -20,6 +20,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libcapsp.so"
+# cuSPARSE SpSV side-by-side used by bench.py only (never by the solve path)
+VENDOR_LIB = BUILD / "libcapsp_vendor.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
@@ -42,11 +44,11 @@ def sources() -> tuple[list[Path], list[Path]]:
 def _deps() -> list[Path]:
     cu, c = sources()
     hdrs = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((CSRC / "host").glob("*.h"))
-    return cu + c + hdrs + [ROOT / "include" / "capsp.h", Path(__file__)]
+    return cu + c + hdrs + list((CSRC / "vendor").glob("*.cu")) + [ROOT / "include" / "capsp.h", Path(__file__)]
 
 
 def up_to_date() -> bool:
-    if not LIB.exists():
+    if not LIB.exists() or (any((CSRC / "vendor").glob("*.cu")) and not VENDOR_LIB.exists()):
         return False
     t = LIB.stat().st_mtime
     return all(p.stat().st_mtime <= t for p in _deps())
@@ -85,7 +87,23 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     os.replace(tmp, LIB)
     if verbose:
         print(f"built {LIB}", file=sys.stderr)
+    build_vendor(nvcc, verbose)
     return LIB
+
+
+def build_vendor(nvcc: str, verbose: bool = False) -> None:
+    """libcapsp_vendor.so (cuSPARSE comparison); optional: a failure only warns."""
+    src = CSRC / "vendor" / "spsv_cusparse.cu"
+    if not src.exists():
+        return
+    tmp = BUILD / "libcapsp_vendor.so.tmp"
+    try:
+        _run([nvcc, *ARCH, *NVCC_FLAGS, "-shared", "-cudart", "static", str(src), "-o", str(tmp), "-lcusparse"])
+        os.replace(tmp, VENDOR_LIB)
+        if verbose:
+            print(f"built {VENDOR_LIB}", file=sys.stderr)
+    except RuntimeError as e:
+        print(f"warning: cuSPARSE comparison library not built: {str(e)[:200]}", file=sys.stderr)
 
 
 if __name__ == "__main__":
