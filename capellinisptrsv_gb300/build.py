@@ -22,6 +22,8 @@ BUILD = PKG / "_build"
 LIB = BUILD / "libcapsp.so"
 # cuSPARSE SpSV side-by-side used by bench.py only (never by the solve path)
 VENDOR_LIB = BUILD / "libcapsp_vendor.so"
+# command-line driver with the reference's main.cu flow and result.csv format
+CLI = BUILD / "capsp_run"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
@@ -44,11 +46,12 @@ def sources() -> tuple[list[Path], list[Path]]:
 def _deps() -> list[Path]:
     cu, c = sources()
     hdrs = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((CSRC / "host").glob("*.h"))
+    hdrs += list((CSRC / "cli").glob("*.c"))
     return cu + c + hdrs + list((CSRC / "vendor").glob("*.cu")) + [ROOT / "include" / "capsp.h", Path(__file__)]
 
 
 def up_to_date() -> bool:
-    if not LIB.exists() or (any((CSRC / "vendor").glob("*.cu")) and not VENDOR_LIB.exists()):
+    if not LIB.exists() or not CLI.exists() or (any((CSRC / "vendor").glob("*.cu")) and not VENDOR_LIB.exists()):
         return False
     t = LIB.stat().st_mtime
     return all(p.stat().st_mtime <= t for p in _deps())
@@ -87,6 +90,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     os.replace(tmp, LIB)
     if verbose:
         print(f"built {LIB}", file=sys.stderr)
+    tmp_cli = BUILD / "capsp_run.tmp"
+    _run(["gcc", "-std=c11", "-O2", "-Wall", "-I", str(ROOT / "include"), str(CSRC / "cli" / "capsp_run.c"),
+          "-L", str(BUILD), "-lcapsp", "-Wl,-rpath,$ORIGIN", "-o", str(tmp_cli)])
+    os.replace(tmp_cli, CLI)
     build_vendor(nvcc, verbose)
     return LIB
 

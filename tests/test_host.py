@@ -237,3 +237,20 @@ def test_batched_generator_is_block_diagonal():
     rows = np.repeat(np.arange(m.n), np.diff(m.rowptr))
     assert np.all(m.colidx >= so[sys_of_row[rows]])
     assert np.all(m.colidx <= rows)
+
+
+def test_cli_usage_and_degenerate_matrix(tmp_path):
+    """capsp_run: bad arguments print usage (exit 2); a 1x1 matrix exits 0 and
+    writes nothing, as the reference's main.cu does for m <= 1 (no GPU needed)."""
+    import subprocess
+    from capellinisptrsv_gb300 import build as B
+    r = subprocess.run([str(B.CLI)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "usage" in r.stderr
+    r = subprocess.run([str(B.CLI), "--alg", "nope", "x.mtx"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2
+    p = tmp_path / "one.mtx"
+    p.write_text("%%MatrixMarket matrix coordinate real general\n1 1 1\n1 1 2.0\n")
+    out = tmp_path / "result.csv"
+    r = subprocess.run([str(B.CLI), "--out", str(out), str(p)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0
+    assert out.exists() and out.read_text() == ""
