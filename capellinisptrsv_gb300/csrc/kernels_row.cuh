@@ -244,6 +244,29 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
     unsigned long long t_first = 0;
     if (a.trace != nullptr)
         t_first = global_timer_ns();
+    // the row is complete: publish into the mirror, the publication vector
+    // and (level schedule) the caller's x
+    auto finish = [&]() {
+        if (a.trace != nullptr && t_ready == 0)
+            t_ready = global_timer_ns();
+        U ub = VB::to(LEVEL ? acc : (bi - acc) * dinv);
+        if (ub == VB::kPending)
+            ub = VB::kQNaN;
+        if (i != a.stuck_row) {
+            cache[(p - lo) * G + g] = ub;
+            st_relaxed(pub + (size_t)pslot * (size_t)pld + g, ub, pol.keep);
+            if (LEVEL)
+                st_stream(reinterpret_cast<U *>(a.x) + (size_t)i * (size_t)a.ld + g, ub, pol.stream);
+            published = true;
+        }
+        if (a.trace != nullptr && g == 0) {
+            a.trace[4 * (size_t)i] = t_pick;
+            a.trace[4 * (size_t)i + 1] = t_first;
+            a.trace[4 * (size_t)i + 2] = t_ready;
+            a.trace[4 * (size_t)i + 3] = global_timer_ns();
+        }
+        done = true;
+    };
     for (;;) {
         // ---- A: polls of dependencies before the chunk ---------------------
         // A fresh batch is swept once: every outstanding dependency polled,
@@ -282,6 +305,14 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
                     changed = true;
                     if (a.trace != nullptr && pend == 0 && j0 + kBatch >= e)
                         t_ready = global_timer_ns();  // last dependency value received
+                    if (pend == 0 && nacc == cnt - 1 && top == (1u << (cnt - 1)) && j0 + kBatch >= e) {
+                        // the row's last dependency, everything before it
+                        // folded: one FMA (same order as the fold) and the row
+                        // publishes now instead of after the warp's B pass
+                        acc = fma(sl.v[(cnt - 1) * 32 + lane], VB::from(u0), acc);
+                        nacc = cnt;
+                        finish();
+                    }
                 } else {
                     int w = 0;
 #pragma unroll
@@ -336,6 +367,7 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
         const bool progress = __any_sync(kFullMask, changed || (!done && pend == 0u));
         // ---- B: in-sub-chunk pickup, fold, publish ------------------------
         if (progress) {
+            __syncwarp();  // mirror stores of rows finished in A visible to the pickups
             for (;;) {
                 const unsigned pubmask = __ballot_sync(kFullMask, published);
                 bool moved = false;
@@ -361,26 +393,7 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
                             load_batch();  // a row with more than kBatch dependencies
                             moved = true;
                         } else {
-                            if (a.trace != nullptr && t_ready == 0)
-                                t_ready = global_timer_ns();
-                            U ub = VB::to(LEVEL ? acc : (bi - acc) * dinv);
-                            if (ub == VB::kPending)
-                                ub = VB::kQNaN;
-                            if (i != a.stuck_row) {
-                                cache[(p - lo) * G + g] = ub;
-                                st_relaxed(pub + (size_t)pslot * (size_t)pld + g, ub, pol.keep);
-                                if (LEVEL)
-                                    st_stream(reinterpret_cast<U *>(a.x) + (size_t)i * (size_t)a.ld + g, ub,
-                                              pol.stream);
-                                published = true;
-                            }
-                            if (a.trace != nullptr && g == 0) {
-                                a.trace[4 * (size_t)i] = t_pick;
-                                a.trace[4 * (size_t)i + 1] = t_first;
-                                a.trace[4 * (size_t)i + 2] = t_ready;
-                                a.trace[4 * (size_t)i + 3] = global_timer_ns();
-                            }
-                            done = true;
+                            finish();
                             moved = true;
                         }
                     }
