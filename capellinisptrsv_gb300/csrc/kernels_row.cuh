@@ -33,7 +33,10 @@
 //   * Polling: a fresh batch of dependencies is swept once; afterwards each
 //     lane probes only the dependency that blocks its in-order fold, and the
 //     next round's probe is issued before the current round folds and
-//     publishes, so the poll's round trip overlaps that work.
+//     publishes, so the poll's round trip overlaps that work.  A row whose
+//     last dependency lands in a probe, with everything before it folded,
+//     takes its one FMA and publishes right there, without waiting for the
+//     warp's fold/publish pass.
 //   * Partial sums are accumulated in storage order whatever the arrival
 //     order, so repeated solves and the WRTFST / TWOPART schedules are
 //     bit-identical.
