@@ -64,6 +64,20 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(values, device):
+    """Element-wise maximum over all ranks (the slowest replica sets the time)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def replica_value(world: int, flops_per_solve: float, max_ms: float) -> float:
+    """Whole-job GFLOP/s of N independent replicas: every rank solves once per step."""
+    return world * flops_per_solve / (max_ms * 1e-3) / 1e9
+
+
 def algorithmic_bytes(n: int, nnz: int, s: int, k: int = 1) -> float:
     """rowptr + colidx + flags + values + b and x (reference formula, k RHS)."""
     return 4.0 * (n + 1) + 4.0 * nnz + 4.0 * n + s * nnz + 2.0 * s * n * k
@@ -329,17 +343,14 @@ def run_native(args):
     ms = sum(step_ms) / len(step_ms)
     kms = sum(kern_ms) / len(kern_ms)
     if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([ms, kms], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms, kms = float(tt[0]), float(tt[1])
+        ms, kms = max_over_ranks([ms, kms], dev)
 
     # correctness spot-check against the reference's self-check (x_ref = ones)
     xh = x_d.cpu().numpy()
     max_dev = float(np.max(np.abs(xh - 1.0)))
 
     flops = 2.0 * m.nnz - m.n
-    value = world * flops / (ms * 1e-3) / 1e9
+    value = replica_value(world, flops, ms)
     alg_bytes = algorithmic_bytes(m.n, m.nnz, s_bytes)
     peak, peak_kind = peaks()
     achieved = alg_bytes / (kms * 1e-3) / 1e9
