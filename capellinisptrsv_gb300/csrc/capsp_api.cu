@@ -698,14 +698,18 @@ static capsp_status_t ensure_column_order(capsp_handle_t h, int backward)
 // warps per SM suit wide levels and two suit narrow ones (more rows in flight
 // than a few levels only add pollers); with G >= 4 lanes per row a warp holds
 // few rows, so every warp the SM can hold in 128-thread blocks pays off.
-static void row_shape(capsp_handle_t h, const Tuning &tn, int nrhs, int *block, int *bps)
+// Wide levels with G >= 4 lanes per row also take the 64-register kernel build
+// (*cap), whatever the shape.
+static void row_shape(capsp_handle_t h, const Tuning &tn, int nrhs, int *block, int *bps, bool *cap = nullptr)
 {
+    const int g = lanes_for_rhs(nrhs);
+    const bool narrow = h->narrow_levels && h->sched == CAPSP_SCHED_LEVEL;
+    if (cap)
+        *cap = g >= 4 && !narrow && h->sched == CAPSP_SCHED_LEVEL;
     *block = tn.block;
     *bps = tn.bps;
     if (!tn.dflt)
         return;
-    const int g = lanes_for_rhs(nrhs);
-    const bool narrow = h->narrow_levels && h->sched == CAPSP_SCHED_LEVEL;
     if (g == 1) {
         *block = narrow ? 64 : 256;
         *bps = 1;
@@ -809,8 +813,9 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs,
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k0, st));
         int blk = 0, bps = 0;
-        row_shape(h, tn, nb, &blk, &bps);
-        CAPSP_CUDA(launch_row_solve<T>(a, kind, tn.R, blk, bps, h->num_sms, st));
+        bool cap = false;
+        row_shape(h, tn, nb, &blk, &bps, &cap);
+        CAPSP_CUDA(launch_row_solve<T>(a, kind, tn.R, blk, bps, h->num_sms, cap, st));
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k1, st));
     }

@@ -87,9 +87,10 @@ inline int lanes_for_rhs(int nrhs)
     return g;
 }
 
+// regcap: the 64-register build of the multi-RHS write-first level kernel
 template <typename T>
 cudaError_t launch_row_solve(const RowArgs<T> &a, int kind, int rows_per_thread, int block,
-                             int blocks_per_sm, int num_sms, cudaStream_t st);
+                             int blocks_per_sm, int num_sms, bool regcap, cudaStream_t st);
 
 template <typename T>
 cudaError_t launch_col_solve(const ColArgs<T> &a, int block, int blocks_per_sm, int num_sms,

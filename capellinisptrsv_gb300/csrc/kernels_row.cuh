@@ -547,8 +547,12 @@ __device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const
     }
 }
 
-template <typename T, int G, int R, int KIND, bool LEVEL>
-__global__ void __launch_bounds__(512) row_solve_kernel(const RowArgs<T> a)
+template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false>
+// CAP limits registers to 64 so that every warp an SM can hold fits: with G >= 4
+// lanes per row on wide levels a warp holds few rows and residency decides
+// (measured on GB300: 16 RHS on wide_4m 2.55 -> 1.84 ms).  Narrow levels and
+// one or two lanes per row run faster with the full register budget.
+__global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const RowArgs<T> a)
 {
     typedef typename VBits<T>::U U;
     constexpr int RPW = 32 / G;
@@ -615,12 +619,12 @@ __global__ void __launch_bounds__(512) row_solve_kernel(const RowArgs<T> a)
 // launch helpers
 // ---------------------------------------------------------------------------
 
-template <typename T, int G, int R, int KIND, bool LEVEL>
+template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false>
 static cudaError_t launch_row_impl(const RowArgs<T> &a, int block, int bps, int num_sms,
                                    cudaStream_t st)
 {
     constexpr int RPW = 32 / G;
-    auto kern = row_solve_kernel<T, G, R, KIND, LEVEL>;
+    auto kern = row_solve_kernel<T, G, R, KIND, LEVEL, CAP>;
     const size_t smem = (size_t)(block / 32) * warp_smem_bytes<T>(R);
     cudaError_t e = cudaSuccess;
     if (smem > 48 * 1024) {
@@ -649,8 +653,12 @@ static cudaError_t launch_row_impl(const RowArgs<T> &a, int block, int bps, int 
 
 template <typename T, int G, bool LEVEL>
 static cudaError_t launch_row_g(const RowArgs<T> &a, int kind, int R, int block, int bps,
-                                int num_sms, cudaStream_t st)
+                                int num_sms, bool cap, cudaStream_t st)
 {
+    if constexpr (G >= 4 && LEVEL) {
+        if (cap && kind == kRowWrtFst && R == 1)
+            return launch_row_impl<T, G, 1, kRowWrtFst, LEVEL, true>(a, block, bps, num_sms, st);
+    }
     if (kind == kRowMix)
         return launch_row_impl<T, G, 1, kRowMix, LEVEL>(a, block, bps, num_sms, st);
     // the two-phase schedule is the reference's single-RHS design; multi-RHS
@@ -673,25 +681,25 @@ static cudaError_t launch_row_g(const RowArgs<T> &a, int kind, int R, int block,
 
 template <typename T, bool LEVEL>
 static cudaError_t launch_row_sched(const RowArgs<T> &a, int kind, int rows_per_thread, int block,
-                                    int blocks_per_sm, int num_sms, cudaStream_t st)
+                                    int blocks_per_sm, int num_sms, bool cap, cudaStream_t st)
 {
     switch (lanes_for_rhs(a.nrhs)) {
-    case 1: return launch_row_g<T, 1, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
-    case 2: return launch_row_g<T, 2, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
-    case 4: return launch_row_g<T, 4, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
-    case 8: return launch_row_g<T, 8, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
-    case 16: return launch_row_g<T, 16, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
-    default: return launch_row_g<T, 32, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
+    case 1: return launch_row_g<T, 1, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, st);
+    case 2: return launch_row_g<T, 2, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, st);
+    case 4: return launch_row_g<T, 4, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, st);
+    case 8: return launch_row_g<T, 8, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, st);
+    case 16: return launch_row_g<T, 16, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, st);
+    default: return launch_row_g<T, 32, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, st);
     }
 }
 
 template <typename T>
 cudaError_t launch_row_solve(const RowArgs<T> &a, int kind, int rows_per_thread, int block,
-                             int blocks_per_sm, int num_sms, cudaStream_t st)
+                             int blocks_per_sm, int num_sms, bool regcap, cudaStream_t st)
 {
     if (a.perm != nullptr)
-        return launch_row_sched<T, true>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
-    return launch_row_sched<T, false>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, st);
+        return launch_row_sched<T, true>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, regcap, st);
+    return launch_row_sched<T, false>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, regcap, st);
 }
 
 // ---------------------------------------------------------------------------
