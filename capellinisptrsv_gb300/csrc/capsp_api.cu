@@ -119,6 +119,7 @@ struct capsp_handle_s {
     std::map<int, MixTable> mix;
     int alg = CAPSP_ALG_AUTO;
     int border = 10;
+    bool border_explicit = false;
     // measured on GB300 (wide-level solves): one chunk per lane, 8 resident
     // warps per SM; more resident warps only add pollers
     Tuning tune = {kRowWrtFst, 1, 256, 1, 10};
@@ -543,6 +544,7 @@ extern "C" capsp_status_t capsp_set_mix_border(capsp_handle_t h, int border)
     std::lock_guard<std::recursive_mutex> lk(h->mu);
     h->border = border;
     h->tune.border = border;
+    h->border_explicit = true;
     h->tuned.clear();
     return CAPSP_OK;
 }
@@ -730,6 +732,12 @@ static Tuning current_tuning(capsp_handle_t h, int nrhs)
     Tuning t = h->tune;
     t.border = h->border;
     t.dflt = !h->tune_explicit;
+    // deep matrices, whose levels are narrower than a warp's 32 rows, have no
+    // row parallelism to spread over lanes: AUTO gives every row a whole warp
+    // (measured on GB300: zipf_1m, 8 rows per level, 177 -> 144 ms)
+    if (h->alg == CAPSP_ALG_AUTO && !h->border_explicit && h->level_built && h->sched == CAPSP_SCHED_LEVEL &&
+        (long long)h->n < 32LL * (long long)h->levels)
+        t.border = 1;
     switch (h->alg) {
     case CAPSP_ALG_TWOPART: t.kind = kRowTwoPart; break;
     case CAPSP_ALG_MIX: t.kind = kRowMix; break;

@@ -446,15 +446,32 @@ __device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const
     const RowView<T, LEVEL> rv(a, p, pol.stream);
     const int i = rv.i;
     const bool active = g < a.nrhs;
-    T bi = T(0);
-    if (active && sl_idx == 0)
+    // The row's newest dependency (last in position order; first in storage
+    // order for the natural upper view) is kept out of the slices: the warp
+    // folds and reduces everything else while it waits, and the lanes of
+    // slice 0 add its term with one FMA when it lands, so a chain through
+    // heavy rows pays one hop per row, not a hop plus a full reduction.
+    const bool upper_nat = !LEVEL && a.upper;
+    const bool has_last = rv.e > rv.s;
+    const int j_last = upper_nat ? rv.s : rv.e - 1;
+    const int rs = (upper_nat && has_last) ? rv.s + 1 : rv.s;
+    const int re = (!upper_nat && has_last) ? rv.e - 1 : rv.e;
+    const bool owner = active && sl_idx == 0;  // lanes that finish the row
+    T bi = T(0), v_last = T(0);
+    int c_last = 0;
+    if (owner) {
         bi = ld_stream(a.b + (size_t)i * (size_t)a.ld + g, pol.stream);
+        if (has_last) {
+            c_last = ld_stream(rv.idx + j_last, pol.stream);
+            v_last = ld_stream(rv.val + j_last, pol.stream);
+        }
+    }
     const U *pb = rv.pub;
     T acc = T(0);
     int c[kBatch];
     unsigned pend = 0;
     int cnt = 0;
-    int j0 = rv.s + sl_idx;
+    int j0 = rs + sl_idx;
     auto load_batch = [&]() {
         pend = 0;
         cnt = 0;
@@ -462,7 +479,7 @@ __device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const
         for (int t = 0; t < kBatch; ++t) {
             const int j = j0 + t * NS;
             c[t] = 0;
-            if (j < rv.e) {
+            if (j < re) {
                 c[t] = ld_stream(rv.idx + j, pol.stream);
                 sl.v[t * 32 + lane] = ld_stream(rv.val + j, pol.stream);
                 pend |= 1u << t;
@@ -470,7 +487,7 @@ __device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const
             }
         }
     };
-    bool done = !active || j0 >= rv.e;
+    bool done = !active || j0 >= re;
     if (!done)
         load_batch();
     bool probe_only = false, aborted = false;
@@ -506,7 +523,7 @@ __device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const
                 for (int t = 0; t < cnt; ++t)
                     acc = fma(sl.v[t * 32 + lane], VB::from(sl.w[t * 32 + lane]), acc);
                 j0 += NS * kBatch;
-                if (j0 < rv.e) {
+                if (j0 < re) {
                     load_batch();
                     probe_only = false;
                 } else {
@@ -529,10 +546,26 @@ __device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const
 #pragma unroll
     for (int off = 16; off >= G; off >>= 1)
         acc += __shfl_xor_sync(kFullMask, acc, off);
+    // the newest dependency: the slice-0 lanes wait for it and finish the row
+    if (owner && has_last && !aborted) {
+        const U *addr = pb + (size_t)c_last * (size_t)rv.pld + g;
+        Spin wait_last;
+        for (;;) {
+            const U u_last = ld_relaxed(addr, pol.keep);
+            if (u_last != VB::kPending) {
+                acc = fma(v_last, VB::from(u_last), acc);
+                break;
+            }
+            if (wait_last.next(a.err, a.wait, i, c_last)) {
+                aborted = true;
+                break;
+            }
+        }
+    }
     unsigned long long t_ready = 0;
     if (a.trace != nullptr)
         t_ready = global_timer_ns();
-    if (sl_idx == 0 && active && i != a.stuck_row) {
+    if (owner && i != a.stuck_row) {
         // level schedule: values are pre-scaled (x = b/d + sum), else x = (b - sum)/d
         U ub = aborted ? VB::kQNaN : VB::to(LEVEL ? fma(bi, rv.dinv, acc) : (bi - acc) * rv.dinv);
         if (ub == VB::kPending)
@@ -547,11 +580,11 @@ __device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const
     }
 }
 
-template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false>
 // CAP limits registers to 64 so that every warp an SM can hold fits: with G >= 4
 // lanes per row on wide levels a warp holds few rows and residency decides
 // (measured on GB300: 16 RHS on wide_4m 2.55 -> 1.84 ms).  Narrow levels and
 // one or two lanes per row run faster with the full register budget.
+template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false>
 __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const RowArgs<T> a)
 {
     typedef typename VBits<T>::U U;
