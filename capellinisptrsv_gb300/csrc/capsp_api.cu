@@ -128,7 +128,9 @@ struct capsp_handle_s {
     // path by default (more rows in flight than a few levels only add pollers)
     bool narrow_levels = false;
     std::map<int, Tuning> tuned;
-    WaitCfg wait = {10000000000ull, 1u << 30, 256u};
+    // no nanosleep backoff by default: measured neutral on wide levels and
+    // 7 % faster on deep chains (zipf_1m), where it delays each detection
+    WaitCfg wait = {10000000000ull, 1u << 30, 0u};
     int stuck_row = -1;
     std::map<GraphKey, cudaGraphExec_t> graphs;
     void *d_stage = nullptr;

@@ -178,7 +178,8 @@ capsp_status_t capsp_set_tuning(capsp_handle_t h, int rows_per_thread,
 capsp_status_t capsp_set_timeout(capsp_handle_t h, uint64_t timeout_ns);
 
 /* Ceiling of the exponential __nanosleep backoff between polls of a pending
- * dependency (default 256 ns; 0 = never sleep). */
+ * dependency (default 0 = never sleep: on GB300 sleeping only delays the
+ * detection of a landed dependency; the wall-clock timeout still bounds it). */
 capsp_status_t capsp_set_backoff(capsp_handle_t h, unsigned sleep_max_ns);
 
 /* Solve op(A) X = B for nrhs right-hand sides (device pointers, element
