@@ -233,6 +233,19 @@ def test_solve_host_buffers(plain20k):
     assert rel_inf_err(x, oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)) <= TOL64
 
 
+@pytest.mark.parametrize("k", [1, 3])
+def test_solve_host_pinned_buffers_in_place(plain20k, k):
+    """Page-locked host buffers are solved in place (no staging copies)."""
+    m = plain20k
+    s = solver_for(m, on_device=False)
+    b = cs.normal(m.n * k, seed=18).reshape(m.n, k) if k > 1 else cs.normal(m.n, seed=18)
+    bh = torch.from_numpy(np.ascontiguousarray(b)).pin_memory()
+    xh = torch.full_like(bh, float("nan")).pin_memory()
+    for _ in range(2):
+        s.solve_host(bh.numpy(), xh.numpy())
+        assert rel_inf_err(xh.numpy(), oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)) <= TOL64
+
+
 def test_graph_replay_and_autotune(plain20k):
     m = plain20k
     s = solver_for(m)
