@@ -53,6 +53,20 @@ __global__ void __launch_bounds__(512) col_solve_kernel(const ColArgs<T> a)
         const int e = a.backward ? e0 - 1 : e0;
         const int need = __ldg(a.indeg + j) - 1;
         const T dinv = __ldg(a.inv_diag + j);
+        // the column's first pass of entries (and, for the fused gradient, the
+        // x values they pair with) do not depend on readiness: fetch them
+        // before the wait so the work after the last arrival hits registers
+        const int k1 = s + es;
+        int r1 = 0;
+        T v1 = T(0);
+        if (k1 < e) {
+            r1 = __ldg(a.idx + k1);
+            v1 = __ldg(a.val + k1);
+        }
+        const int kg1 = s0 + es;
+        T xg1 = T(0);
+        if (a.grad_val != nullptr && kg1 < e0 && active)
+            xg1 = __ldg(a.xf + (size_t)__ldg(a.idx + kg1) * (size_t)a.ld + g);
         bool aborted = false;
         T xj = T(0);
         if (es == 0 && active) {
@@ -72,17 +86,17 @@ __global__ void __launch_bounds__(512) col_solve_kernel(const ColArgs<T> a)
         }
         xj = __shfl_sync(kFullMask, xj, g);
         if (j != a.stuck_row) {
-            for (int k = s + es; k < e; k += EPW) {
-                const int r = __ldg(a.idx + k);
-                const T v = __ldg(a.val + k);
+            for (int k = k1; k < e; k += EPW) {
+                const int r = k == k1 ? r1 : __ldg(a.idx + k);
+                const T v = k == k1 ? v1 : __ldg(a.val + k);
                 if (active)
                     atomicAdd(a.left_sum + (size_t)r * (size_t)a.lsld + g, xj * v);
             }
             __threadfence();
             __syncwarp();
             if (g == 0) {
-                for (int k = s + es; k < e; k += EPW)
-                    atomicAdd(a.arrived + __ldg(a.idx + k), 1);
+                for (int k = k1; k < e; k += EPW)
+                    atomicAdd(a.arrived + (k == k1 ? r1 : __ldg(a.idx + k)), 1);
             }
         }
         if (a.grad_val != nullptr) {
@@ -90,7 +104,7 @@ __global__ void __launch_bounds__(512) col_solve_kernel(const ColArgs<T> a)
                 const int k = kb + es;
                 T prod = T(0);
                 if (k < e0 && active)
-                    prod = xj * __ldg(a.xf + (size_t)__ldg(a.idx + k) * (size_t)a.ld + g);
+                    prod = xj * (k == kg1 ? xg1 : __ldg(a.xf + (size_t)__ldg(a.idx + k) * (size_t)a.ld + g));
 #pragma unroll
                 for (int off = G / 2; off >= 1; off >>= 1)
                     prod += __shfl_xor_sync(kFullMask, prod, off);
