@@ -781,6 +781,11 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs,
         const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
         int kind = tn.kind;
         MixTable *mt = nullptr;
+        // AUTO with 8+ lanes per row: a heavy row would get only 32/G slices,
+        // too few to pay for the warp's reduction (measured on GB300: grad_1m
+        // 16 RHS 1.34 ms mixed, 1.13 ms thread-per-row)
+        if (kind < 0 && lanes_for_rhs(nb) >= 8)
+            kind = kRowWrtFst;
         if (kind == kRowMix || kind < 0) {
             CAPSP_TRY(ensure_mix(h, group_rows_for(nb), tn.border, &mt));
             if (kind < 0)
