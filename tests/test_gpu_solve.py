@@ -192,6 +192,38 @@ def test_zipf_mix_path(schedule):
     assert rel_inf_err(x, xo) <= TOL64
 
 
+@pytest.mark.parametrize("k", [1, 4])
+def test_auto_deep_matrix_gives_every_row_a_warp(k):
+    """Levels narrower than 32 rows: AUTO runs every row warp-per-row (the row's
+    newest dependency folded last), single and multi-RHS."""
+    m = cs.generate("zipf_1m", seed=0, n=200_000)
+    b = cs.normal(m.n * k, seed=31).reshape(m.n, k) if k > 1 else cs.normal(m.n, seed=31)
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
+    s = solver_for(m)
+    for _ in range(2):
+        x = host(s.solve(dev(b)))
+        s.status()
+        assert rel_inf_err(x, xo) <= TOL64
+    if k == 1:  # info() describes the single-RHS launch
+        assert s.info()["warp_occupy"] == pytest.approx(1.0)
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+@pytest.mark.parametrize("k", [1, 2])
+def test_upper_csr_warp_per_row(schedule, k):
+    """Upper CSR through the warp-per-row kernel (border 1: every row), where the
+    natural schedule's newest dependency is the first stored entry."""
+    m = cs.generate(n=20_000, kmin=1, kmax=12, band=700, seed=6)
+    cp, ri, cv = cs.matrix_transposition(m.n, m.n, m.nnz, m.rowptr, m.colidx, m.val)
+    g = cs.normal(m.n * k, seed=32).reshape(m.n, k) if k > 1 else cs.normal(m.n, seed=32)
+    yo = oracle.solve_csr_transpose(m.rowptr, m.colidx, m.val, g)
+    s = cs.TriangularSolver(dev(cp), dev(ri), dev(cv), uplo="upper", algorithm="mix", schedule=schedule)
+    s.set_mix_border(1)
+    y = host(s.solve(dev(g)))
+    s.status()
+    assert rel_inf_err(y, yo) <= TOL64
+
+
 @pytest.mark.parametrize("schedule", SCHEDULES)
 def test_upper_csr_and_csc_paths(schedule):
     """Upper-triangular CSR (backward substitution) and the CSC warp-per-column
