@@ -44,7 +44,8 @@
 //     level schedule pre-scales the values instead (x = b/d + sum (-v/d) x_j),
 //     so a single FMA follows the last dependency.
 //   * Multi-RHS: G = next_pow2(nrhs) lanes share a row, one right-hand side
-//     each; every (row, rhs) element is published and polled independently.
+//     each (more than 16: 8 lanes with RPL = 4 right-hand sides each); every
+//     (row, rhs) element is published and polled independently.
 //   * Every wait is bounded (Spin); a lane that gives up publishes a quiet
 //     NaN so its dependants finish, and the error word records TIMEOUT.
 #pragma once
@@ -136,12 +137,14 @@ struct Slots {
     int *q;                        // dependency positions
 };
 
-// bytes of dynamic shared memory per warp: chunk mirror + slot storage
+// bytes of dynamic shared memory per warp: chunk mirror (32R elements of RPL
+// right-hand sides) + slot storage (kBatch / RPL dependencies of RPL values)
 template <typename T>
-__host__ __device__ constexpr size_t warp_smem_bytes(int R)
+__host__ __device__ constexpr size_t warp_smem_bytes(int R, int RPL = 1)
 {
-    return (size_t)32 * R * sizeof(typename VBits<T>::U) +
-           (size_t)kBatch * 32 * (sizeof(T) + sizeof(typename VBits<T>::U) + sizeof(int));
+    return (size_t)32 * R * RPL * sizeof(typename VBits<T>::U) +
+           (size_t)(kBatch / RPL) * 32 * (sizeof(T) + sizeof(int)) +
+           (size_t)kBatch * 32 * sizeof(typename VBits<T>::U);
 }
 
 // Convergent chunk solve.  The warp's chunk holds schedule positions
@@ -164,7 +167,7 @@ __host__ __device__ constexpr size_t warp_smem_bytes(int R)
 // warp-wide DFMA occupies an SM sub-partition's FP64 pipe for ~64 cycles).
 // TWO (the two-phase schedule of the reference's our2Part) polls the outside
 // dependencies one at a time in storage order.
-template <typename T, int G, bool TWO, bool LEVEL>
+template <typename T, int G, bool TWO, bool LEVEL, int RPL>
 __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, const int sub, const int p,
                                            const bool mine, const int g,
                                            volatile typename VBits<T>::U *cache, const Slots<T> &sl,
@@ -173,10 +176,16 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
     typedef VBits<T> VB;
     typedef typename VB::U U;
     const int lane = threadIdx.x & 31;
+    constexpr int KB = kBatch / RPL;       // dependencies in flight per lane (RPL values each)
+    const int r0 = g * RPL;                // this lane's first right-hand side
+    const int nq = mine ? min(RPL, a.nrhs - r0) : 0;
     int i = 0, j0 = 0, e = 0;
     const int *idxp = nullptr;
     const T *valp = nullptr;
-    T dinv = T(0), bi = T(0), acc = T(0);
+    T dinv = T(0), bi[RPL], acc[RPL];
+#pragma unroll
+    for (int r = 0; r < RPL; ++r)
+        bi[r] = acc[r] = T(0);
     U *pub = nullptr;
     long long pld = 0, pslot = 0;
     if (mine) {
@@ -190,21 +199,25 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
         pub = rv.pub;
         pld = rv.pld;
         pslot = rv.pslot;
-        bi = ld_stream(a.b + (size_t)i * (size_t)a.ld + g, pol.stream);
-        if (LEVEL)
-            acc = bi * dinv;  // x = b/d + sum (-v/d) x_j
+#pragma unroll
+        for (int r = 0; r < RPL; ++r) {
+            if (r < nq)
+                bi[r] = ld_stream(a.b + (size_t)i * (size_t)a.ld + r0 + r, pol.stream);
+            if (LEVEL)
+                acc[r] = bi[r] * dinv;  // x = b/d + sum (-v/d) x_j
+        }
     }
-    int c[kBatch];                    // dependency index (position, or row in natural order)
+    int c[KB];                    // dependency index (position, or row in natural order)
     unsigned pend = 0, ext = 0, need = 0;
     int nacc = 0, cnt = 0;
     bool sweep_next = false;          // a fresh batch is swept once, then probed
     auto load_batch = [&]() {
         sweep_next = true;
-        cnt = min(kBatch, e - j0);
+        cnt = min(KB, e - j0);
         pend = ext = need = 0;
         nacc = 0;
 #pragma unroll
-        for (int t = 0; t < kBatch; ++t) {
+        for (int t = 0; t < KB; ++t) {
             c[t] = 0;
             if (t < cnt) {
                 const int cc = ld_stream(idxp + j0 + t, pol.stream);
@@ -216,7 +229,9 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
                     ext |= 1u << t;
                     pend |= 1u << t;
                 } else if (q < sub) {  // earlier sub-chunk of this chunk: already in the mirror
-                    sl.w[t * 32 + lane] = cache[(q - lo) * G + g];
+#pragma unroll
+                    for (int r = 0; r < RPL; ++r)
+                        sl.w[(t * RPL + r) * 32 + lane] = cache[((q - lo) * G + g) * RPL + r];
                 } else {
                     pend |= 1u << t;
                     need |= 1u << ((q - sub) * G + g);
@@ -230,15 +245,22 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
     auto fold = [&]() {
         const int lim = pend ? __ffs(pend) - 1 : cnt;
 #pragma unroll 1
-        for (int t = nacc; t < lim; ++t)
-            acc = fma(sl.v[t * 32 + lane], VB::from(sl.w[t * 32 + lane]), acc);
+        for (int t = nacc; t < lim; ++t) {
+            const T v = sl.v[t * 32 + lane];
+#pragma unroll
+            for (int r = 0; r < RPL; ++r)
+                acc[r] = fma(v, VB::from(sl.w[(t * RPL + r) * 32 + lane]), acc[r]);
+        }
         nacc = lim;
     };
     bool done = !mine, published = !mine;
     if (mine && j0 < e)
         load_batch();
     bool aborted = false;
-    U u_next = VB::kPending;          // probe issued at the end of the previous round
+    U u_next[RPL];                    // probe issued at the end of the previous round
+#pragma unroll
+    for (int r = 0; r < RPL; ++r)
+        u_next[r] = VB::kPending;
     unsigned top_next = 0u;           // ... and the slot it polls
     unsigned long long t_ready = 0;
     Spin sp;
@@ -252,14 +274,19 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
     auto finish = [&]() {
         if (a.trace != nullptr && t_ready == 0)
             t_ready = global_timer_ns();
-        U ub = VB::to(LEVEL ? acc : (bi - acc) * dinv);
-        if (ub == VB::kPending)
-            ub = VB::kQNaN;
         if (i != a.stuck_row) {
-            cache[(p - lo) * G + g] = ub;
-            st_relaxed(pub + (size_t)pslot * (size_t)pld + g, ub, pol.keep);
-            if (LEVEL)
-                st_stream(reinterpret_cast<U *>(a.x) + (size_t)i * (size_t)a.ld + g, ub, pol.stream);
+#pragma unroll
+            for (int r = 0; r < RPL; ++r) {
+                if (r < nq) {
+                    U ub = VB::to(LEVEL ? acc[r] : (bi[r] - acc[r]) * dinv);
+                    if (ub == VB::kPending)
+                        ub = VB::kQNaN;
+                    cache[((p - lo) * G + g) * RPL + r] = ub;
+                    st_relaxed(pub + (size_t)pslot * (size_t)pld + r0 + r, ub, pol.keep);
+                    if (LEVEL)
+                        st_stream(reinterpret_cast<U *>(a.x) + (size_t)i * (size_t)a.ld + r0 + r, ub, pol.stream);
+                }
+            }
             published = true;
         }
         if (a.trace != nullptr && g == 0) {
@@ -289,37 +316,53 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
         if (!__any_sync(kFullMask, sweep)) {
             // probe round (warp-uniform): the value polled at the end of the
             // previous round when it was for this slot, else a fresh load
-            U u0 = u_next;
+            U u0[RPL];
+#pragma unroll
+            for (int r = 0; r < RPL; ++r)
+                u0[r] = u_next[r];
             if (top != 0u && top != top_next) {
                 const U *addr = pub;
 #pragma unroll
-                for (int t = 0; t < kBatch; ++t)
+                for (int t = 0; t < KB; ++t)
                     if ((top >> t) & 1u)
-                        addr = pub + (size_t)c[t] * (size_t)pld + g;
-                u0 = ld_relaxed(addr, pol.keep);
-            }
-            if (top) {
-                if (u0 != VB::kPending) {
+                        addr = pub + (size_t)c[t] * (size_t)pld + r0;
 #pragma unroll
-                    for (int t = 0; t < kBatch; ++t)
-                        if ((top >> t) & 1u)
-                            sl.w[t * 32 + lane] = u0;
+                for (int r = 0; r < RPL; ++r)
+                    u0[r] = r < nq ? ld_relaxed(addr + r, pol.keep) : (U)0;
+            }
+            bool landed = true;
+#pragma unroll
+            for (int r = 0; r < RPL; ++r)
+                landed = landed && (r >= nq || u0[r] != VB::kPending);
+            if (top) {
+                if (landed) {
+#pragma unroll
+                    for (int t = 0; t < KB; ++t)
+                        if ((top >> t) & 1u) {
+#pragma unroll
+                            for (int r = 0; r < RPL; ++r)
+                                sl.w[(t * RPL + r) * 32 + lane] = u0[r];
+                        }
                     pend &= ~top;
                     changed = true;
-                    if (a.trace != nullptr && pend == 0 && j0 + kBatch >= e)
+                    if (a.trace != nullptr && pend == 0 && j0 + KB >= e)
                         t_ready = global_timer_ns();  // last dependency value received
-                    if (pend == 0 && nacc == cnt - 1 && top == (1u << (cnt - 1)) && j0 + kBatch >= e) {
+                    if (pend == 0 && nacc == cnt - 1 && top == (1u << (cnt - 1)) && j0 + KB >= e) {
                         // the row's last dependency, everything before it
-                        // folded: one FMA (same order as the fold) and the row
-                        // publishes now instead of after the warp's B pass
-                        acc = fma(sl.v[(cnt - 1) * 32 + lane], VB::from(u0), acc);
+                        // folded: one FMA per right-hand side (same order as
+                        // the fold) and the row publishes now instead of after
+                        // the warp's B pass
+                        const T v = sl.v[(cnt - 1) * 32 + lane];
+#pragma unroll
+                        for (int r = 0; r < RPL; ++r)
+                            acc[r] = fma(v, VB::from(u0[r]), acc[r]);
                         nacc = cnt;
                         finish();
                     }
                 } else {
                     int w = 0;
 #pragma unroll
-                    for (int t = 0; t < kBatch; ++t)
+                    for (int t = 0; t < KB; ++t)
                         if ((top >> t) & 1u)
                             w = c[t];
                     waited = w;
@@ -329,17 +372,26 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
             // sweep round: every outstanding outside dependency, all loads in
             // flight together before any result is consumed (in-order issue
             // would otherwise stall on the first result)
-            U u[kBatch];
+            U u[KB][RPL];
 #pragma unroll
-            for (int t = 0; t < kBatch; ++t)
-                u[t] = ((ext_pend >> t) & 1u) ? ld_relaxed(pub + (size_t)c[t] * (size_t)pld + g, pol.keep)
-                                              : VB::kPending;
+            for (int t = 0; t < KB; ++t)
+#pragma unroll
+                for (int r = 0; r < RPL; ++r)
+                    u[t][r] = ((ext_pend >> t) & 1u) && r < nq
+                                  ? ld_relaxed(pub + (size_t)c[t] * (size_t)pld + r0 + r, pol.keep)
+                                  : (U)0;
             unsigned got = 0;
 #pragma unroll
-            for (int t = 0; t < kBatch; ++t) {
+            for (int t = 0; t < KB; ++t) {
                 if ((ext_pend >> t) & 1u) {
-                    if (u[t] != VB::kPending) {
-                        sl.w[t * 32 + lane] = u[t];
+                    bool ok = true;
+#pragma unroll
+                    for (int r = 0; r < RPL; ++r)
+                        ok = ok && u[t][r] != VB::kPending;
+                    if (ok) {
+#pragma unroll
+                        for (int r = 0; r < RPL; ++r)
+                            sl.w[(t * RPL + r) * 32 + lane] = u[t][r];
                         got |= 1u << t;
                     } else {
                         waited = c[t];
@@ -348,7 +400,7 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
             }
             pend &= ~got;
             changed = changed || got != 0;
-            if (a.trace != nullptr && got != 0 && pend == 0 && j0 + kBatch >= e)
+            if (a.trace != nullptr && got != 0 && pend == 0 && j0 + KB >= e)
                 t_ready = global_timer_ns();  // last dependency value received
         }
         {
@@ -356,14 +408,18 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
             // a batch loaded in B is swept instead)
             const unsigned np = done ? 0u : (pend & ext);
             top_next = np & (0u - np);
-            u_next = VB::kPending;
+#pragma unroll
+            for (int r = 0; r < RPL; ++r)
+                u_next[r] = VB::kPending;
             if (top_next != 0u) {
                 const U *addr = pub;
 #pragma unroll
-                for (int t = 0; t < kBatch; ++t)
+                for (int t = 0; t < KB; ++t)
                     if ((top_next >> t) & 1u)
-                        addr = pub + (size_t)c[t] * (size_t)pld + g;
-                u_next = ld_relaxed(addr, pol.keep);
+                        addr = pub + (size_t)c[t] * (size_t)pld + r0;
+#pragma unroll
+                for (int r = 0; r < RPL; ++r)
+                    u_next[r] = r < nq ? ld_relaxed(addr + r, pol.keep) : (U)0;
             }
         }
         // a lane whose current batch is complete but not yet folded also needs B
@@ -382,7 +438,9 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
                             m &= m - 1;
                             const int q = sl.q[t * 32 + lane];
                             if ((pubmask >> ((q - sub) * G + g)) & 1u) {
-                                sl.w[t * 32 + lane] = cache[(q - lo) * G + g];
+#pragma unroll
+                                for (int r = 0; r < RPL; ++r)
+                                    sl.w[(t * RPL + r) * 32 + lane] = cache[((q - lo) * G + g) * RPL + r];
                                 pend &= ~(1u << t);
                             }
                         }
@@ -391,9 +449,9 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
                     if (nacc < cnt)
                         fold();
                     if (pend == 0 && nacc >= cnt) {
-                        j0 += kBatch;
+                        j0 += KB;
                         if (j0 < e) {
-                            load_batch();  // a row with more than kBatch dependencies
+                            load_batch();  // a row with more than KB dependencies
                             moved = true;
                         } else {
                             finish();
@@ -421,10 +479,16 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
         if (__any_sync(kFullMask, aborted)) {
             // give up: unfinished rows publish a quiet NaN so their dependants end
             if (!done && i != a.stuck_row) {
-                cache[(p - lo) * G + g] = VB::kQNaN;
-                st_relaxed(pub + (size_t)pslot * (size_t)pld + g, VB::kQNaN, pol.keep);
-                if (LEVEL)
-                    st_stream(reinterpret_cast<U *>(a.x) + (size_t)i * (size_t)a.ld + g, VB::kQNaN, pol.stream);
+#pragma unroll
+                for (int r = 0; r < RPL; ++r) {
+                    if (r < nq) {
+                        cache[((p - lo) * G + g) * RPL + r] = VB::kQNaN;
+                        st_relaxed(pub + (size_t)pslot * (size_t)pld + r0 + r, VB::kQNaN, pol.keep);
+                        if (LEVEL)
+                            st_stream(reinterpret_cast<U *>(a.x) + (size_t)i * (size_t)a.ld + r0 + r, VB::kQNaN,
+                                      pol.stream);
+                    }
+                }
             }
             __syncwarp();
             break;
@@ -584,20 +648,23 @@ __device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const
 // lanes per row on wide levels a warp holds few rows and residency decides
 // (measured on GB300: 16 RHS on wide_4m 2.55 -> 1.84 ms).  Narrow levels and
 // one or two lanes per row run faster with the full register budget.
-template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false>
+// RPL: right-hand sides per lane (G lanes per row cover G * RPL of them), so a
+// warp holds 32 / G rows however many right-hand sides there are.
+template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false, int RPL = 1>
 __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const RowArgs<T> a)
 {
     typedef typename VBits<T>::U U;
+    static_assert(RPL == 1 || KIND == kRowWrtFst, "several right-hand sides per lane: write-first only");
     constexpr int RPW = 32 / G;
     constexpr int CH = RPW * R;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    unsigned char *wbase = smem_raw + (size_t)wib * warp_smem_bytes<T>(R);
+    unsigned char *wbase = smem_raw + (size_t)wib * warp_smem_bytes<T>(R, RPL);
     volatile U *cache = reinterpret_cast<volatile U *>(wbase);
     Slots<T> sl;
-    sl.v = reinterpret_cast<T *>(wbase + (size_t)32 * R * sizeof(U));
-    sl.w = reinterpret_cast<U *>(sl.v + kBatch * 32);
+    sl.v = reinterpret_cast<T *>(wbase + (size_t)32 * R * RPL * sizeof(U));
+    sl.w = reinterpret_cast<U *>(sl.v + (kBatch / RPL) * 32);
     sl.q = reinterpret_cast<int *>(sl.w + kBatch * 32);
     const int rl = lane / G, g = lane % G;
     L2Pol pol;
@@ -619,15 +686,15 @@ __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const Row
                 break;
             const int lo = (int)tk;
 #pragma unroll
-            for (int r = 0; r < R; ++r)
+            for (int r = 0; r < R * RPL; ++r)
                 cache[r * 32 + lane] = VBits<T>::kPending;
             __syncwarp();
 #pragma unroll 1
             for (int r = 0; r < R; ++r) {
                 const int sub = lo + r * RPW;
                 const int p = sub + rl;
-                chunk_rows<T, G, KIND == kRowTwoPart, LEVEL>(a, lo, sub, p, p < a.n && g < a.nrhs, g, cache, sl,
-                                                             t_pick, pol);
+                chunk_rows<T, G, KIND == kRowTwoPart, LEVEL, RPL>(a, lo, sub, p, p < a.n && g * RPL < a.nrhs, g,
+                                                                  cache, sl, t_pick, pol);
             }
             __syncwarp();
         } else {
@@ -638,7 +705,7 @@ __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const Row
                 cache[lane] = VBits<T>::kPending;
                 __syncwarp();
                 const int p = lo + rl;
-                chunk_rows<T, G, false, LEVEL>(a, lo, lo, p, p < hi && g < a.nrhs, g, cache, sl, t_pick, pol);
+                chunk_rows<T, G, false, LEVEL, 1>(a, lo, lo, p, p < hi && g < a.nrhs, g, cache, sl, t_pick, pol);
                 __syncwarp();
             } else {
                 warp_row<T, G, LEVEL>(a, lo, rl, g, sl, pol);
@@ -652,13 +719,13 @@ __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const Row
 // launch helpers
 // ---------------------------------------------------------------------------
 
-template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false>
+template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false, int RPL = 1>
 static cudaError_t launch_row_impl(const RowArgs<T> &a, int block, int bps, int num_sms,
                                    cudaStream_t st)
 {
     constexpr int RPW = 32 / G;
-    auto kern = row_solve_kernel<T, G, R, KIND, LEVEL, CAP>;
-    const size_t smem = (size_t)(block / 32) * warp_smem_bytes<T>(R);
+    auto kern = row_solve_kernel<T, G, R, KIND, LEVEL, CAP, RPL>;
+    const size_t smem = (size_t)(block / 32) * warp_smem_bytes<T>(R, RPL);
     cudaError_t e = cudaSuccess;
     if (smem > 48 * 1024) {
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -712,10 +779,27 @@ static cudaError_t launch_row_g(const RowArgs<T> &a, int kind, int R, int block,
     }
 }
 
+// Write-first launches with more than 16 right-hand sides pack four of them
+// per lane: 8 lanes per row instead of 32, so a warp keeps 4 rows in flight
+// instead of 1 (measured on GB300: wide_4m with 32 RHS 3.34 -> 2.75 ms).  With
+// fewer right-hand sides a lane per right-hand side is faster: the packed
+// lane's serial loads, stores and FMAs lengthen every round (4 RHS: 1.02 ms
+// unpacked, 1.92 ms packed).
+template <typename T, bool LEVEL>
+static cudaError_t launch_row_packed(const RowArgs<T> &a, int block, int bps, int num_sms, bool cap,
+                                     cudaStream_t st)
+{
+    if (cap)
+        return launch_row_impl<T, 8, 1, kRowWrtFst, LEVEL, true, 4>(a, block, bps, num_sms, st);
+    return launch_row_impl<T, 8, 1, kRowWrtFst, LEVEL, false, 4>(a, block, bps, num_sms, st);
+}
+
 template <typename T, bool LEVEL>
 static cudaError_t launch_row_sched(const RowArgs<T> &a, int kind, int rows_per_thread, int block,
                                     int blocks_per_sm, int num_sms, bool cap, cudaStream_t st)
 {
+    if (kind == kRowWrtFst && rows_per_thread == 1 && a.nrhs > 16)
+        return launch_row_packed<T, LEVEL>(a, block, blocks_per_sm, num_sms, cap, st);
     switch (lanes_for_rhs(a.nrhs)) {
     case 1: return launch_row_g<T, 1, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, st);
     case 2: return launch_row_g<T, 2, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, st);
