@@ -737,9 +737,17 @@ static Tuning current_tuning(capsp_handle_t h, int nrhs)
     // deep matrices, whose levels are narrower than a warp's 32 rows, have no
     // row parallelism to spread over lanes: AUTO gives every row a whole warp
     // (measured on GB300: zipf_1m, 8 rows per level, 177 -> 144 ms)
-    if (h->alg == CAPSP_ALG_AUTO && !h->border_explicit && h->level_built && h->sched == CAPSP_SCHED_LEVEL &&
-        (long long)h->n < 32LL * (long long)h->levels)
-        t.border = 1;
+    // Otherwise AUTO gives a row group a warp per row only when its rows hold
+    // a warp's worth of entries on average: shorter rows run faster one per
+    // lane (measured on GB300: 2,048 banded systems with 4-13 entries per row,
+    // mixed at the reference's border of 10: 2.98 ms; one lane per row:
+    // 1.96 ms).
+    if (h->alg == CAPSP_ALG_AUTO && !h->border_explicit) {
+        if (h->level_built && h->sched == CAPSP_SCHED_LEVEL && (long long)h->n < 32LL * (long long)h->levels)
+            t.border = 1;
+        else if (t.border < 32)
+            t.border = 32;
+    }
     switch (h->alg) {
     case CAPSP_ALG_TWOPART: t.kind = kRowTwoPart; break;
     case CAPSP_ALG_MIX: t.kind = kRowMix; break;

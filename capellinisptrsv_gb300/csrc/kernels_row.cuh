@@ -54,7 +54,9 @@
 
 namespace capsp {
 
-constexpr int kBatch = 8;  // dependencies one lane keeps in flight
+// dependencies one lane keeps in flight (the level schedule in
+// host/preprocess.c sorts rows by this pass size: CAPSP_ROW_PASS)
+constexpr int kBatch = 8;
 
 // Where a row's data lives, for the natural and the level schedule.
 template <typename T, bool LEVEL>

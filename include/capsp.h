@@ -416,9 +416,10 @@ int capsp_mix_table(int n, const int *rowptr, int upper, int group_rows, int bor
 /* Level schedule of a triangular matrix read row by row in solve order
  * (rows 0..n-1 with the diagonal last, or with upper != 0 rows n-1..0 with the
  * diagonal first): level = 1 + deepest dependency level (the recurrence of
- * matrix_layer); order[k] = k-th row of a stable sort by level, position =
- * its inverse; level_start (optional, n+2 ints) = first position of each
- * level.  Returns the level count or -1. */
+ * matrix_layer); order[k] = k-th row of a sort by level and, inside a level,
+ * by dependency count, most first (ties in solve order); position = its
+ * inverse; level_start (optional, n+2 ints) = first position of each level.
+ * Returns the level count or -1. */
 int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *order,
                          int *position, int *level_start);
 

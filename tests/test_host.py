@@ -176,7 +176,7 @@ def test_row_levels_histogram():
 @pytest.mark.parametrize("upper", [False, True])
 def test_level_schedule_is_a_topological_level_order(upper):
     from capellinisptrsv_gb300.solver import level_layout, level_schedule
-    m = cs.generate(n=4000, kmin=0, kmax=6, band=300, seed=6)
+    m = cs.generate(n=4000, kmin=0, kmax=12, band=300, seed=6)
     rp, ci, v = m.rowptr, m.colidx, m.val
     if upper:  # the CSC of L is the CSR of U = L^T (diagonal first)
         rp, ci, v = cs.matrix_transposition(m.n, m.n, m.nnz, m.rowptr, m.colidx, m.val)
@@ -196,6 +196,22 @@ def test_level_schedule_is_a_topological_level_order(upper):
     # levels are contiguous blocks of positions
     lev_of_pos = np.repeat(np.arange(1, levels + 1), np.diff(start[1:levels + 2]))
     assert np.all(np.diff(lev_of_pos) >= 0)
+    # inside a level holding a row of more than 8 dependencies (one pass of the
+    # row kernel): dependency count non-increasing (63+ in one bucket), ties in
+    # solve order; any other level keeps solve order
+    ndep = np.minimum(np.diff(rp)[order] - 1, 63)
+    solve_rank = (m.n - 1 - order) if upper else order
+    sorted_levels = 0
+    for l in range(1, levels + 1):
+        a, b = start[l], start[l + 1]
+        d, r = ndep[a:b], solve_rank[a:b]
+        if d.size and d.max() > 8:
+            sorted_levels += 1
+            assert np.all(np.diff(d) <= 0)
+            assert np.all((np.diff(d) < 0) | (np.diff(r) > 0))
+        else:
+            assert np.all(np.diff(r) > 0)
+    assert 0 < sorted_levels < levels
 
 
 def _validate(rp, ci, fmt=N.FMT_CSR, uplo=N.LOWER):
