@@ -1078,9 +1078,16 @@ extern "C" capsp_status_t capsp_solve_host(capsp_handle_t h, const void *b_host,
     // the coherent CPU-GPU link, so the H2D copy disappears (measured on
     // GB300 + Grace: wide_4m e2e 1.14 -> 1.05 ms).  x stays staged: the rows
     // finish scattered over x, and scattered stores to host memory were
-    // slower than one D2H copy (1.49 ms).
-    void *b_in_place = (h->format == CAPSP_FMT_CSR && h->sched == CAPSP_SCHED_LEVEL) ? pinned_alias(b_host)
-                                                                                      : nullptr;
+    // slower than one D2H copy (1.49 ms).  Levels of 32k rows and more keep
+    // the GPU busy without waiting, and then a single right-hand side, 8 bytes
+    // per scattered read over the link, costs more than the copy (2,048
+    // systems with 93k rows per level: 5.66 ms in place, 4.80 ms copied; with
+    // 4 right-hand sides, 32 bytes per read, 8.97 ms in place, 11.2 copied).
+    const bool throughput_bound = h->level_built && (long long)h->n >= 32768LL * (long long)h->levels;
+    void *b_in_place = (h->format == CAPSP_FMT_CSR && h->sched == CAPSP_SCHED_LEVEL &&
+                        !(throughput_bound && nrhs == 1))
+                           ? pinned_alias(b_host)
+                           : nullptr;
     if (b_in_place) {
         CAPSP_TRY(dispatch(h, kOpSolve, b_in_place, dx, nullptr, nullptr, nrhs, nrhs, st));
     } else {

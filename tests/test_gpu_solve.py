@@ -278,6 +278,31 @@ def test_solve_host_pinned_buffers_in_place(plain20k, k):
         assert rel_inf_err(xh.numpy(), oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)) <= TOL64
 
 
+@pytest.mark.parametrize("k", [1, 2])
+def test_solve_host_pinned_buffers_wide_levels(k):
+    """Two levels of 35,000 rows (wider than the 32k rows at which a single
+    right-hand side is copied rather than read in place), pinned buffers."""
+    n = 70_000
+    rng = np.random.default_rng(41)
+    odd = np.arange(n) % 2 == 1
+    rowptr = np.concatenate([[0], np.cumsum(np.where(odd, 2, 1))]).astype(np.int32)
+    colidx = np.empty(rowptr[-1], np.int32)
+    val = np.empty(rowptr[-1])
+    off = rng.uniform(-1, 1, n)
+    colidx[rowptr[:-1][odd]] = np.arange(n)[odd] - 1
+    val[rowptr[:-1][odd]] = off[odd]
+    colidx[rowptr[1:] - 1] = np.arange(n)
+    val[rowptr[1:] - 1] = 1 + np.where(odd, np.abs(off), 0)
+    assert cs.matrix_layer(n, n, len(colidx), rowptr, colidx)[0] == 2
+    s = cs.TriangularSolver(rowptr, colidx, val)
+    b = cs.normal(n * k, seed=42).reshape(n, k) if k > 1 else cs.normal(n, seed=42)
+    bh = torch.from_numpy(np.ascontiguousarray(b)).pin_memory()
+    xh = torch.full_like(bh, float("nan")).pin_memory()
+    for _ in range(2):
+        s.solve_host(bh.numpy(), xh.numpy())
+        assert rel_inf_err(xh.numpy(), oracle.solve_csr_lower(rowptr, colidx, val, b)) <= TOL64
+
+
 def test_graph_replay_and_autotune(plain20k):
     m = plain20k
     s = solver_for(m)
