@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-vendor", action="store_true", help="skip the cuSPARSE SpSV side-by-side")
+    ap.add_argument("--nsys", type=int, default=0, help="systems in the batched workload (default 2,048)")
     return ap.parse_args()
 
 
@@ -196,7 +197,7 @@ def run_reference_forms(args):
     import capellinisptrsv_gb300 as cs
     if args.workload == "batched":
         k = args.nrhs or BATCH_KS[0]
-        m = cs.generate_batched(BATCH_NSYS, seed=0)
+        m = cs.generate_batched(args.nsys or BATCH_NSYS, seed=0)
         nsys = len(m.sys_rowoff) - 1
         picks = sorted(set(np.linspace(0, nsys - 1, 64).round().astype(int).tolist()))
         rhs = _batch_rhs(cs, m.n, k)
@@ -535,7 +536,7 @@ def run_batched(args):
     _single_gpu_forms(args)
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    m = cs.generate_batched(BATCH_NSYS, seed=0)
+    m = cs.generate_batched(args.nsys or BATCH_NSYS, seed=0)
     nsys = len(m.sys_rowoff) - 1
     to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
     rp_d, ci_d, val_d = to(m.rowptr), to(m.colidx), to(m.val)
@@ -632,8 +633,10 @@ def run_batched(args):
         }
         entry["speedup_vs_loop"] = entry["solves_per_s"] / entry["loop_solves_per_s"]
         alg = algorithmic_bytes(m.n, m.nnz, 8, k)
+        # DRAM bytes per launch from the committed capture (single RHS, default batch)
+        traffic = profile_traffic("row_solve", "batched_f64") if k == 1 and nsys == BATCH_NSYS else None
         entry["roofline"] = {"bound": "hbm", "achieved": alg / (kms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-                             "frac": alg / (kms * 1e-3) / 1e9 / peak, "traffic": None, "peak_kind": peak_kind,
+                             "frac": alg / (kms * 1e-3) / 1e9 / peak, "traffic": traffic, "peak_kind": peak_kind,
                              "kernel": "row_solve_kernel", "kernel_ms": kms, "algorithmic_bytes_per_launch": alg}
         sweep.append(entry)
         del b_d, x_d, cols, calls
@@ -790,8 +793,10 @@ def run_autograd(args):
     else:
         roof = {"kernel": "row_solve_kernel (forward)", "kernel_ms": kf,
                 "algorithmic_bytes_per_launch": fwd_bytes, "achieved": fwd_bytes / (kf * 1e-3) / 1e9}
+    # DRAM bytes of the captured column launch (grad_1m, 16 RHS) when that is the one reported
+    traffic = profile_traffic("col_solve", f"grad_1m_{k}rhs_f64") if kb >= kf else None
     roof.update({"bound": "hbm", "peak": peak, "unit": "GB/s", "frac": roof["achieved"] / peak,
-                 "traffic": None, "peak_kind": peak_kind})
+                 "traffic": traffic, "peak_kind": peak_kind})
     cpu = None
     if not args.no_cpu_baseline:
         cpu = _cpu_autograd(m, b_h, xs_h, args.cpu_seconds)

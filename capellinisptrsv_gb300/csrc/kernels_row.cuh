@@ -181,6 +181,10 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
     constexpr int KB = kBatch / RPL;       // dependencies in flight per lane (RPL values each)
     const int r0 = g * RPL;                // this lane's first right-hand side
     const int nq = mine ? min(RPL, a.nrhs - r0) : 0;
+    // right-hand side r of this lane exists; with one per lane that is implied
+    // wherever it is asked (only lanes that own a row load, store or poll), and
+    // the test compiles away (keeping it cost the single-RHS solve 2-5 %)
+    const auto has_rhs = [nq](int r) { return RPL == 1 || r < nq; };
     int i = 0, j0 = 0, e = 0;
     const int *idxp = nullptr;
     const T *valp = nullptr;
@@ -203,7 +207,7 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
         pslot = rv.pslot;
 #pragma unroll
         for (int r = 0; r < RPL; ++r) {
-            if (r < nq)
+            if (has_rhs(r))
                 bi[r] = ld_stream(a.b + (size_t)i * (size_t)a.ld + r0 + r, pol.stream);
             if (LEVEL)
                 acc[r] = bi[r] * dinv;  // x = b/d + sum (-v/d) x_j
@@ -279,7 +283,7 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
         if (i != a.stuck_row) {
 #pragma unroll
             for (int r = 0; r < RPL; ++r) {
-                if (r < nq) {
+                if (has_rhs(r)) {
                     U ub = VB::to(LEVEL ? acc[r] : (bi[r] - acc[r]) * dinv);
                     if (ub == VB::kPending)
                         ub = VB::kQNaN;
@@ -330,12 +334,12 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
                         addr = pub + (size_t)c[t] * (size_t)pld + r0;
 #pragma unroll
                 for (int r = 0; r < RPL; ++r)
-                    u0[r] = r < nq ? ld_relaxed(addr + r, pol.keep) : (U)0;
+                    u0[r] = has_rhs(r) ? ld_relaxed(addr + r, pol.keep) : (U)0;
             }
             bool landed = true;
 #pragma unroll
             for (int r = 0; r < RPL; ++r)
-                landed = landed && (r >= nq || u0[r] != VB::kPending);
+                landed = landed && (!has_rhs(r) || u0[r] != VB::kPending);
             if (top) {
                 if (landed) {
 #pragma unroll
@@ -379,7 +383,7 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
             for (int t = 0; t < KB; ++t)
 #pragma unroll
                 for (int r = 0; r < RPL; ++r)
-                    u[t][r] = ((ext_pend >> t) & 1u) && r < nq
+                    u[t][r] = ((ext_pend >> t) & 1u) && has_rhs(r)
                                   ? ld_relaxed(pub + (size_t)c[t] * (size_t)pld + r0 + r, pol.keep)
                                   : (U)0;
             unsigned got = 0;
@@ -421,7 +425,7 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
                         addr = pub + (size_t)c[t] * (size_t)pld + r0;
 #pragma unroll
                 for (int r = 0; r < RPL; ++r)
-                    u_next[r] = r < nq ? ld_relaxed(addr + r, pol.keep) : (U)0;
+                    u_next[r] = has_rhs(r) ? ld_relaxed(addr + r, pol.keep) : (U)0;
             }
         }
         // a lane whose current batch is complete but not yet folded also needs B
@@ -483,7 +487,7 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
             if (!done && i != a.stuck_row) {
 #pragma unroll
                 for (int r = 0; r < RPL; ++r) {
-                    if (r < nq) {
+                    if (has_rhs(r)) {
                         cache[((p - lo) * G + g) * RPL + r] = VB::kQNaN;
                         st_relaxed(pub + (size_t)pslot * (size_t)pld + r0 + r, VB::kQNaN, pol.keep);
                         if (LEVEL)
