@@ -101,6 +101,8 @@ static inline int64_t row_k(const capsp_gen_params_t *p, const zipf_t *z, rng_t 
     int64_t k;
     if (p->kind == CAPSP_GEN_ZIPF_NEAR_FAR) {
         k = zipf_draw(z, r);
+        if (k < p->kmin) /* optional floor on the drawn count */
+            k = p->kmin;
         if (k > i)
             k = i;
     } else {
@@ -165,7 +167,8 @@ static int check_params(const capsp_gen_params_t *p)
     if (p->kind == CAPSP_GEN_UNIFORM_BAND)
         return p->kmin >= 0 && p->kmax >= p->kmin && p->kmax < GEN_MAX_K;
     if (p->kind == CAPSP_GEN_ZIPF_NEAR_FAR)
-        return p->zipf_cap >= 1 && p->zipf_cap < GEN_MAX_K && p->zipf_s > 0.0 && p->near_window >= 1;
+        return p->zipf_cap >= 1 && p->zipf_cap < GEN_MAX_K && p->zipf_s > 0.0 && p->near_window >= 1 &&
+               p->kmin >= 0 && p->kmin < GEN_MAX_K;
     return 0;
 }
 

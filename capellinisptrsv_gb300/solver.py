@@ -84,7 +84,12 @@ WORKLOADS = {
     # n=4,194,304; k~U{1..7} (mean 4) in [max(0,i-65536), i-1]; b = L*ones
     "wide_4m": dict(n=4_194_304, kind=N.GEN_UNIFORM_BAND, kmin=1, kmax=7, band=65536),
     # n=1,048,576; k~Zipf(1.8) on 1..512; ceil(k/2) cols in [i-32, i-1], the rest in [0, i-1]
+    # (a literal Zipf(1.8): 6.96 off-diagonals per row on average, ~126k levels)
     "zipf_1m": dict(n=1_048_576, kind=N.GEN_ZIPF_NEAR_FAR, zipf_s=1.8, zipf_cap=512, near_window=32),
+    # the same with the count floored at 38, which brings the mean to ~40 off-diagonals
+    # per row; 19 of the previous 32 rows per row make it a near-serial chain
+    "zipf40_1m": dict(n=1_048_576, kind=N.GEN_ZIPF_NEAR_FAR, kmin=38, zipf_s=1.8, zipf_cap=512,
+                      near_window=32),
     # n=1,048,576; k~U{2..10} (mean 6) in a band of 16,384 (differentiation workload)
     "grad_1m": dict(n=1_048_576, kind=N.GEN_UNIFORM_BAND, kmin=2, kmax=10, band=16384),
 }

@@ -453,7 +453,8 @@ int read_mtx_f32(const char *filename, int *m_add, int *n_add, int *nnzA_add,
  * (seed, stream, row), so the result is independent of thread count. */
 typedef enum capsp_gen_kind {
     CAPSP_GEN_UNIFORM_BAND = 0, /* k ~ U{kmin..kmax}, distinct cols uniform in [max(0,i-band), i-1] */
-    CAPSP_GEN_ZIPF_NEAR_FAR = 1 /* k ~ Zipf(s) on 1..cap; ceil(k/2) cols in [i-near, i-1], rest uniform in [0, i-1] */
+    CAPSP_GEN_ZIPF_NEAR_FAR = 1 /* k ~ max(kmin, Zipf(s) on 1..cap); ceil(k/2) cols in [i-near, i-1]
+                                   (at most near of them), the rest uniform in [0, i-1] */
 } capsp_gen_kind_t;
 
 typedef struct capsp_gen_params {

@@ -192,6 +192,20 @@ def test_zipf_mix_path(schedule):
     assert rel_inf_err(x, xo) <= TOL64
 
 
+def test_zipf40_near_serial_chain():
+    """The Zipf workload with its count floored at 38 (~40 off-diagonals per row,
+    about 1.5 rows per level): AUTO, FP64, against the oracle."""
+    m = cs.generate("zipf40_1m", seed=0, n=60_000)
+    b = cs.normal(m.n, seed=40)
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
+    s = solver_for(m)
+    for _ in range(2):
+        x = host(s.solve(dev(b)))
+        s.status()
+        assert rel_inf_err(x, xo) <= TOL64
+    assert s.info()["levels"] > m.n // 2
+
+
 @pytest.mark.parametrize("k", [1, 4])
 def test_auto_deep_matrix_gives_every_row_a_warp(k):
     """Levels narrower than 32 rows: AUTO runs every row warp-per-row (the row's

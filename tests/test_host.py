@@ -100,6 +100,22 @@ def test_zipf_generator_near_far_rule():
     assert np.sum(cols >= i - 32) >= (k + 1) // 2
 
 
+def test_zipf_generator_count_floor():
+    """kmin floors the Zipf count (zipf40_1m: mean ~40 off-diagonals per row); the
+    default floor of 1 leaves the literal draw unchanged."""
+    kw = dict(n=20_000, kind=N.GEN_ZIPF_NEAR_FAR, zipf_s=1.8, zipf_cap=512, near_window=32, seed=1)
+    lit = cs.generate(**kw)
+    assert cs.generate(kmin=1, **kw).digest() == lit.digest()
+    m = cs.generate(kmin=38, **kw)
+    ks = np.diff(m.rowptr) - 1
+    rows = np.arange(m.n)
+    assert np.all(ks == np.minimum(np.maximum(np.diff(lit.rowptr) - 1, 38), rows))
+    assert 38 < ks[1000:].mean() < 43
+    i = 10_000
+    cols = m.colidx[m.rowptr[i]:m.rowptr[i + 1] - 1]
+    assert np.sum(cols >= i - 32) >= min((len(cols) + 1) // 2, 32)
+
+
 def test_normal_generator_moments():
     z = cs.normal(200_000, seed=5)
     assert abs(z.mean()) < 0.01 and abs(z.std() - 1.0) < 0.01
