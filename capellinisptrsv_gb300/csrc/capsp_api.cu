@@ -267,10 +267,14 @@ static capsp_status_t build_level(capsp_handle_t h)
     const size_t vb = h->vbytes;
     CAPSP_CUDA(cudaMalloc(&h->d_perm, sizeof(int) * (size_t)n));
     CAPSP_CUDA(cudaMalloc(&h->d_lptr, sizeof(int) * ((size_t)n + 1)));
-    CAPSP_CUDA(cudaMalloc(&h->d_lidx, sizeof(int) * lidx.size()));
+    // 4 entries of padding: the row kernels stage a chunk's entries in 16-byte
+    // pieces from a 16-byte boundary, up to 3 entries past its last one
+    CAPSP_CUDA(cudaMalloc(&h->d_lidx, sizeof(int) * (lidx.size() + 4)));
     CAPSP_CUDA(cudaMalloc(&h->d_lsrc, sizeof(int) * lsrc.size()));
     CAPSP_CUDA(cudaMalloc(&h->d_dsrc, sizeof(int) * (size_t)n));
-    CAPSP_CUDA(cudaMalloc(&h->d_lval, vb * lidx.size()));
+    CAPSP_CUDA(cudaMalloc(&h->d_lval, vb * (lidx.size() + 4)));
+    CAPSP_CUDA(cudaMemset(h->d_lidx + lidx.size(), 0, sizeof(int) * 4));
+    CAPSP_CUDA(cudaMemset((char *)h->d_lval + vb * lidx.size(), 0, vb * 4));
     CAPSP_CUDA(cudaMalloc(&h->d_linv, vb * (size_t)n));
     CAPSP_CUDA(cudaMemcpy(h->d_perm, order.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
     CAPSP_CUDA(cudaMemcpy(h->d_lptr, lptr.data(), sizeof(int) * ((size_t)n + 1), cudaMemcpyHostToDevice));
@@ -704,6 +708,13 @@ static capsp_status_t ensure_column_order(capsp_handle_t h, int backward)
 // few rows, so every warp the SM can hold in 128-thread blocks pays off.
 // Wide levels with G >= 4 lanes per row also take the 64-register kernel build
 // (*cap), whatever the shape.
+// Levels of 32k rows and more on average keep the GPU busy without waiting on
+// the dependency chain: the solve is then bound by throughput, not latency.
+static bool wide_levels(capsp_handle_t h)
+{
+    return h->level_built && (long long)h->n >= 32768LL * (long long)h->levels;
+}
+
 static void row_shape(capsp_handle_t h, const Tuning &tn, int nrhs, int *block, int *bps, bool *cap = nullptr)
 {
     const int g = lanes_for_rhs(nrhs);
@@ -838,7 +849,13 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs,
         int blk = 0, bps = 0;
         bool cap = false;
         row_shape(h, tn, nb, &blk, &bps, &cap);
-        CAPSP_CUDA(launch_row_solve<T>(a, kind, tn.R, blk, bps, h->num_sms, cap, st));
+        // One lane per row stages each sub-chunk's entries in shared memory
+        // with coalesced copies, which shortens the dependency hops of
+        // latency-bound solves (measured on GB300: wide_4m 0.792 -> 0.771 ms,
+        // grad_1m 1.324 -> 1.311 ms) but slows throughput-bound ones (2,048
+        // systems with 93k rows per level: 1.66 -> 2.34 ms).
+        const bool stage = level && nb == 1 && !wide_levels(h);
+        CAPSP_CUDA(launch_row_solve<T>(a, kind, tn.R, blk, bps, h->num_sms, cap, stage, st));
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k1, st));
     }
@@ -1083,9 +1100,8 @@ extern "C" capsp_status_t capsp_solve_host(capsp_handle_t h, const void *b_host,
     // per scattered read over the link, costs more than the copy (2,048
     // systems with 93k rows per level: 5.66 ms in place, 4.80 ms copied; with
     // 4 right-hand sides, 32 bytes per read, 8.97 ms in place, 11.2 copied).
-    const bool throughput_bound = h->level_built && (long long)h->n >= 32768LL * (long long)h->levels;
     void *b_in_place = (h->format == CAPSP_FMT_CSR && h->sched == CAPSP_SCHED_LEVEL &&
-                        !(throughput_bound && nrhs == 1))
+                        !(wide_levels(h) && nrhs == 1))
                            ? pinned_alias(b_host)
                            : nullptr;
     if (b_in_place) {

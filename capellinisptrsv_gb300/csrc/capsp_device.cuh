@@ -163,6 +163,21 @@ __device__ __forceinline__ unsigned long long global_timer_ns()
     return t;
 }
 
+// 16-byte asynchronous global -> shared copy (both addresses 16-byte aligned),
+// L2 policy as for the streamed loads.  Completion: cp_async_wait_all().
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, unsigned long long pol)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(s), "l"(gmem), "l"(pol)
+                 : "memory");
+}
+
+// commit this thread's outstanding cp.async copies and wait for all of them
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 // Budget of one dependency wait.
 struct WaitCfg {
     unsigned long long timeout_ns;  // wall-clock budget of a single wait

@@ -87,10 +87,12 @@ inline int lanes_for_rhs(int nrhs)
     return g;
 }
 
-// regcap: the 64-register build of the multi-RHS write-first level kernel
+// regcap: the 64-register build of the multi-RHS write-first level kernel;
+// stage: one lane per row on the level schedule with each 32-row sub-chunk's
+// entries staged in shared memory (ignored for other launches)
 template <typename T>
 cudaError_t launch_row_solve(const RowArgs<T> &a, int kind, int rows_per_thread, int block,
-                             int blocks_per_sm, int num_sms, bool regcap, cudaStream_t st);
+                             int blocks_per_sm, int num_sms, bool regcap, bool stage, cudaStream_t st);
 
 template <typename T>
 cudaError_t launch_col_solve(const ColArgs<T> &a, int block, int blocks_per_sm, int num_sms,

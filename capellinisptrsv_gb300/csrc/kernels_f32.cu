@@ -5,7 +5,8 @@
 
 namespace capsp {
 
-template cudaError_t launch_row_solve<float>(const RowArgs<float> &, int, int, int, int, int, bool, cudaStream_t);
+template cudaError_t launch_row_solve<float>(const RowArgs<float> &, int, int, int, int, int, bool, bool,
+                                                cudaStream_t);
 template cudaError_t launch_col_solve<float>(const ColArgs<float> &, int, int, int, cudaStream_t);
 template cudaError_t launch_fill_pending<float>(float *, int, int, long long, unsigned *, int, int *,
                                               cudaStream_t);

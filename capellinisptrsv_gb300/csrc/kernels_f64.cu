@@ -5,7 +5,8 @@
 
 namespace capsp {
 
-template cudaError_t launch_row_solve<double>(const RowArgs<double> &, int, int, int, int, int, bool, cudaStream_t);
+template cudaError_t launch_row_solve<double>(const RowArgs<double> &, int, int, int, int, int, bool, bool,
+                                                cudaStream_t);
 template cudaError_t launch_col_solve<double>(const ColArgs<double> &, int, int, int, cudaStream_t);
 template cudaError_t launch_fill_pending<double>(double *, int, int, long long, unsigned *, int, int *,
                                               cudaStream_t);

@@ -137,16 +137,24 @@ struct Slots {
     T *v;                          // dependency values, [t * 32 + lane]
     typename VBits<T>::U *w;       // received x values
     int *q;                        // dependency positions
+    int *si;                       // staged entries of the sub-chunk: positions ...
+    T *sv;                         // ... and values (staged launches only)
 };
+
+// Entries of a 32-row sub-chunk staged in shared memory (STAGE launches: one
+// lane per row, level schedule): up to kStage of them, from a 16-byte boundary.
+constexpr int kStage = 384;
 
 // bytes of dynamic shared memory per warp: chunk mirror (32R elements of RPL
 // right-hand sides) + slot storage (kBatch / RPL dependencies of RPL values)
+// + the staging buffers.  Every part is a multiple of 16 bytes.
 template <typename T>
-__host__ __device__ constexpr size_t warp_smem_bytes(int R, int RPL = 1)
+__host__ __device__ constexpr size_t warp_smem_bytes(int R, int RPL = 1, bool stage = false)
 {
     return (size_t)32 * R * RPL * sizeof(typename VBits<T>::U) +
            (size_t)(kBatch / RPL) * 32 * (sizeof(T) + sizeof(int)) +
-           (size_t)kBatch * 32 * sizeof(typename VBits<T>::U);
+           (size_t)kBatch * 32 * sizeof(typename VBits<T>::U) +
+           (stage ? (size_t)kStage * (sizeof(int) + sizeof(T)) : 0);
 }
 
 // Convergent chunk solve.  The warp's chunk holds schedule positions
@@ -169,7 +177,7 @@ __host__ __device__ constexpr size_t warp_smem_bytes(int R, int RPL = 1)
 // warp-wide DFMA occupies an SM sub-partition's FP64 pipe for ~64 cycles).
 // TWO (the two-phase schedule of the reference's our2Part) polls the outside
 // dependencies one at a time in storage order.
-template <typename T, int G, bool TWO, bool LEVEL, int RPL>
+template <typename T, int G, bool TWO, bool LEVEL, int RPL, bool STAGE>
 __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, const int sub, const int p,
                                            const bool mine, const int g,
                                            volatile typename VBits<T>::U *cache, const Slots<T> &sl,
@@ -213,6 +221,30 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
                 acc[r] = bi[r] * dinv;  // x = b/d + sum (-v/d) x_j
         }
     }
+    // Stage the sub-chunk's entries.  Its rows' entries are consecutive in the
+    // level layout, so 16-byte copies by all lanes read them with full sectors;
+    // a lane walking its own row touches a different line with every load.
+    int sbase = 0;
+    bool staged = false;
+    static_assert(!STAGE || (LEVEL && G == 1 && RPL == 1), "staging: one lane per row, level schedule");
+    if constexpr (STAGE) {
+        const int lo_e = __reduce_min_sync(kFullMask, mine ? j0 : INT_MAX);
+        const int hi_e = __reduce_max_sync(kFullMask, mine ? e : INT_MIN);
+        const int s4 = lo_e & ~3, e4 = (hi_e + 3) & ~3;  // 16-byte boundaries of the positions
+        if (hi_e > lo_e && e4 - s4 <= kStage) {
+            staged = true;
+            sbase = s4;
+            const int nidx = (e4 - s4) / 4;
+            const int nval = (e4 - s4) * (int)sizeof(T) / 16;
+            for (int k = lane; k < nidx; k += 32)
+                cp_async16(sl.si + 4 * k, a.lidx + s4 + 4 * k, pol.stream);
+            for (int k = lane; k < nval; k += 32)
+                cp_async16(reinterpret_cast<char *>(sl.sv) + 16 * k,
+                           reinterpret_cast<const char *>(a.lval + s4) + 16 * k, pol.stream);
+            cp_async_wait_all();
+        }
+        __syncwarp();
+    }
     int c[KB];                    // dependency index (position, or row in natural order)
     unsigned pend = 0, ext = 0, need = 0;
     int nacc = 0, cnt = 0;
@@ -226,10 +258,10 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
         for (int t = 0; t < KB; ++t) {
             c[t] = 0;
             if (t < cnt) {
-                const int cc = ld_stream(idxp + j0 + t, pol.stream);
+                const int cc = staged ? sl.si[j0 + t - sbase] : ld_stream(idxp + j0 + t, pol.stream);
                 const int q = LEVEL ? cc : (a.upper ? a.n - 1 - cc : cc);
                 c[t] = cc;
-                sl.v[t * 32 + lane] = ld_stream(valp + j0 + t, pol.stream);
+                sl.v[t * 32 + lane] = staged ? sl.sv[j0 + t - sbase] : ld_stream(valp + j0 + t, pol.stream);
                 sl.q[t * 32 + lane] = q;
                 if (q < lo) {
                     ext |= 1u << t;
@@ -656,7 +688,7 @@ __device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const
 // one or two lanes per row run faster with the full register budget.
 // RPL: right-hand sides per lane (G lanes per row cover G * RPL of them), so a
 // warp holds 32 / G rows however many right-hand sides there are.
-template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false, int RPL = 1>
+template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false, int RPL = 1, bool STAGE = false>
 __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const RowArgs<T> a)
 {
     typedef typename VBits<T>::U U;
@@ -666,12 +698,14 @@ __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const Row
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    unsigned char *wbase = smem_raw + (size_t)wib * warp_smem_bytes<T>(R, RPL);
+    unsigned char *wbase = smem_raw + (size_t)wib * warp_smem_bytes<T>(R, RPL, STAGE);
     volatile U *cache = reinterpret_cast<volatile U *>(wbase);
     Slots<T> sl;
     sl.v = reinterpret_cast<T *>(wbase + (size_t)32 * R * RPL * sizeof(U));
     sl.w = reinterpret_cast<U *>(sl.v + (kBatch / RPL) * 32);
     sl.q = reinterpret_cast<int *>(sl.w + kBatch * 32);
+    sl.si = sl.q + (kBatch / RPL) * 32;
+    sl.sv = reinterpret_cast<T *>(sl.si + kStage);
     const int rl = lane / G, g = lane % G;
     L2Pol pol;
     pol.stream = l2_policy_evict_first();
@@ -699,7 +733,7 @@ __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const Row
             for (int r = 0; r < R; ++r) {
                 const int sub = lo + r * RPW;
                 const int p = sub + rl;
-                chunk_rows<T, G, KIND == kRowTwoPart, LEVEL, RPL>(a, lo, sub, p, p < a.n && g * RPL < a.nrhs, g,
+                chunk_rows<T, G, KIND == kRowTwoPart, LEVEL, RPL, STAGE>(a, lo, sub, p, p < a.n && g * RPL < a.nrhs, g,
                                                                   cache, sl, t_pick, pol);
             }
             __syncwarp();
@@ -711,7 +745,8 @@ __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const Row
                 cache[lane] = VBits<T>::kPending;
                 __syncwarp();
                 const int p = lo + rl;
-                chunk_rows<T, G, false, LEVEL, 1>(a, lo, lo, p, p < hi && g < a.nrhs, g, cache, sl, t_pick, pol);
+                chunk_rows<T, G, false, LEVEL, 1, STAGE>(a, lo, lo, p, p < hi && g < a.nrhs, g, cache, sl, t_pick,
+                                                        pol);
                 __syncwarp();
             } else {
                 warp_row<T, G, LEVEL>(a, lo, rl, g, sl, pol);
@@ -725,13 +760,13 @@ __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const Row
 // launch helpers
 // ---------------------------------------------------------------------------
 
-template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false, int RPL = 1>
+template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false, int RPL = 1, bool STAGE = false>
 static cudaError_t launch_row_impl(const RowArgs<T> &a, int block, int bps, int num_sms,
                                    cudaStream_t st)
 {
     constexpr int RPW = 32 / G;
-    auto kern = row_solve_kernel<T, G, R, KIND, LEVEL, CAP, RPL>;
-    const size_t smem = (size_t)(block / 32) * warp_smem_bytes<T>(R, RPL);
+    auto kern = row_solve_kernel<T, G, R, KIND, LEVEL, CAP, RPL, STAGE>;
+    const size_t smem = (size_t)(block / 32) * warp_smem_bytes<T>(R, RPL, STAGE);
     cudaError_t e = cudaSuccess;
     if (smem > 48 * 1024) {
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -757,10 +792,35 @@ static cudaError_t launch_row_impl(const RowArgs<T> &a, int block, int bps, int 
     return cudaGetLastError();
 }
 
+// one lane per row on the level schedule, entries staged in shared memory
+template <typename T>
+static cudaError_t launch_row_staged(const RowArgs<T> &a, int kind, int R, int block, int bps, int num_sms,
+                                     cudaStream_t st)
+{
+    if (kind == kRowMix)
+        return launch_row_impl<T, 1, 1, kRowMix, true, false, 1, true>(a, block, bps, num_sms, st);
+    if (kind == kRowTwoPart) {
+        switch (R) {
+        case 4: return launch_row_impl<T, 1, 4, kRowTwoPart, true, false, 1, true>(a, block, bps, num_sms, st);
+        case 2: return launch_row_impl<T, 1, 2, kRowTwoPart, true, false, 1, true>(a, block, bps, num_sms, st);
+        default: return launch_row_impl<T, 1, 1, kRowTwoPart, true, false, 1, true>(a, block, bps, num_sms, st);
+        }
+    }
+    switch (R) {
+    case 4: return launch_row_impl<T, 1, 4, kRowWrtFst, true, false, 1, true>(a, block, bps, num_sms, st);
+    case 2: return launch_row_impl<T, 1, 2, kRowWrtFst, true, false, 1, true>(a, block, bps, num_sms, st);
+    default: return launch_row_impl<T, 1, 1, kRowWrtFst, true, false, 1, true>(a, block, bps, num_sms, st);
+    }
+}
+
 template <typename T, int G, bool LEVEL>
 static cudaError_t launch_row_g(const RowArgs<T> &a, int kind, int R, int block, int bps,
-                                int num_sms, bool cap, cudaStream_t st)
+                                int num_sms, bool cap, bool stage, cudaStream_t st)
 {
+    if constexpr (G == 1 && LEVEL) {
+        if (stage)
+            return launch_row_staged<T>(a, kind, R, block, bps, num_sms, st);
+    }
     if constexpr (G >= 4 && LEVEL) {
         if (cap && kind == kRowWrtFst && R == 1)
             return launch_row_impl<T, G, 1, kRowWrtFst, LEVEL, true>(a, block, bps, num_sms, st);
@@ -802,27 +862,28 @@ static cudaError_t launch_row_packed(const RowArgs<T> &a, int block, int bps, in
 
 template <typename T, bool LEVEL>
 static cudaError_t launch_row_sched(const RowArgs<T> &a, int kind, int rows_per_thread, int block,
-                                    int blocks_per_sm, int num_sms, bool cap, cudaStream_t st)
+                                    int blocks_per_sm, int num_sms, bool cap, bool stage, cudaStream_t st)
 {
     if (kind == kRowWrtFst && rows_per_thread == 1 && a.nrhs > 16)
         return launch_row_packed<T, LEVEL>(a, block, blocks_per_sm, num_sms, cap, st);
     switch (lanes_for_rhs(a.nrhs)) {
-    case 1: return launch_row_g<T, 1, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, st);
-    case 2: return launch_row_g<T, 2, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, st);
-    case 4: return launch_row_g<T, 4, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, st);
-    case 8: return launch_row_g<T, 8, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, st);
-    case 16: return launch_row_g<T, 16, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, st);
-    default: return launch_row_g<T, 32, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, st);
+    case 1: return launch_row_g<T, 1, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, stage, st);
+    case 2: return launch_row_g<T, 2, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, stage, st);
+    case 4: return launch_row_g<T, 4, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, stage, st);
+    case 8: return launch_row_g<T, 8, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, stage, st);
+    case 16: return launch_row_g<T, 16, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, stage, st);
+    default: return launch_row_g<T, 32, LEVEL>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, cap, stage, st);
     }
 }
 
 template <typename T>
 cudaError_t launch_row_solve(const RowArgs<T> &a, int kind, int rows_per_thread, int block,
-                             int blocks_per_sm, int num_sms, bool regcap, cudaStream_t st)
+                             int blocks_per_sm, int num_sms, bool regcap, bool stage, cudaStream_t st)
 {
     if (a.perm != nullptr)
-        return launch_row_sched<T, true>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, regcap, st);
-    return launch_row_sched<T, false>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, regcap, st);
+        return launch_row_sched<T, true>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, regcap, stage,
+                                         st);
+    return launch_row_sched<T, false>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, regcap, false, st);
 }
 
 // ---------------------------------------------------------------------------
