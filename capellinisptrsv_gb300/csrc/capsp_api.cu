@@ -851,10 +851,12 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs,
         row_shape(h, tn, nb, &blk, &bps, &cap);
         // One lane per row stages each sub-chunk's entries in shared memory
         // with coalesced copies, which shortens the dependency hops of
-        // latency-bound solves (measured on GB300: wide_4m 0.792 -> 0.771 ms,
-        // grad_1m 1.324 -> 1.311 ms) but slows throughput-bound ones (2,048
-        // systems with 93k rows per level: 1.66 -> 2.34 ms).
-        const bool stage = level && nb == 1 && !wide_levels(h);
+        // latency-bound FP64 solves (measured on GB300: wide_4m 0.792 -> 0.771
+        // ms, grad_1m 1.324 -> 1.311 ms) but slows throughput-bound ones
+        // (2,048 systems with 93k rows per level: 1.66 -> 2.34 ms).  FP32
+        // entries are 8 bytes, and there it was mixed (wide_4m 0.715 -> 0.730
+        // ms, grad_1m 1.242 -> 1.230 ms), so FP32 walks the rows directly.
+        const bool stage = level && nb == 1 && !wide_levels(h) && sizeof(T) == 8;
         CAPSP_CUDA(launch_row_solve<T>(a, kind, tn.R, blk, bps, h->num_sms, cap, stage, st));
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k1, st));

@@ -89,7 +89,7 @@ inline int lanes_for_rhs(int nrhs)
 
 // regcap: the 64-register build of the multi-RHS write-first level kernel;
 // stage: one lane per row on the level schedule with each 32-row sub-chunk's
-// entries staged in shared memory (ignored for other launches)
+// entries staged in shared memory (FP64 only; ignored for other launches)
 template <typename T>
 cudaError_t launch_row_solve(const RowArgs<T> &a, int kind, int rows_per_thread, int block,
                              int blocks_per_sm, int num_sms, bool regcap, bool stage, cudaStream_t st);

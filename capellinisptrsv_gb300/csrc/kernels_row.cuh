@@ -817,7 +817,7 @@ template <typename T, int G, bool LEVEL>
 static cudaError_t launch_row_g(const RowArgs<T> &a, int kind, int R, int block, int bps,
                                 int num_sms, bool cap, bool stage, cudaStream_t st)
 {
-    if constexpr (G == 1 && LEVEL) {
+    if constexpr (G == 1 && LEVEL && sizeof(T) == 8) {
         if (stage)
             return launch_row_staged<T>(a, kind, R, block, bps, num_sms, st);
     }
