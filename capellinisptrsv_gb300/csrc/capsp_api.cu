@@ -629,6 +629,11 @@ static capsp_status_t ensure_mix(capsp_handle_t h, int group_rows, int border, M
     return CAPSP_OK;
 }
 
+// Column-driven solves keep each target's partial sum and arrival count in one
+// atomic word (col_solve_packed_kernel) instead of a left_sum array, a counter
+// array and a fence between them.
+constexpr bool kPackedColumns = true;
+
 static capsp_status_t ensure_column_scratch(capsp_handle_t h, int nrhs)
 {
     if (!h->d_indeg) {
@@ -644,7 +649,9 @@ static capsp_status_t ensure_column_scratch(capsp_handle_t h, int nrhs)
         cudaFree(h->d_left);
         h->d_left = nullptr;
         h->left_cap = 0;
-        CAPSP_CUDA(cudaMalloc(&h->d_left, h->vbytes * (size_t)h->n * (size_t)want));
+        // twice the left_sum size: the column kernels keep a sum-and-count
+        // word (two values' width) per element
+        CAPSP_CUDA(cudaMalloc(&h->d_left, 2 * h->vbytes * (size_t)h->n * (size_t)want));
         h->left_cap = want;
     }
     return CAPSP_OK;
@@ -873,8 +880,12 @@ static capsp_status_t enqueue_cols(capsp_handle_t h, const T *b, T *x, int nrhs,
     CAPSP_TRY(ensure_column_order(h, backward));
     for (int r0 = 0; r0 < nrhs; r0 += 32) {
         const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
-        CAPSP_CUDA(cudaMemsetAsync(h->d_arrived, 0, sizeof(int) * (size_t)h->n, st));
-        CAPSP_CUDA(cudaMemsetAsync(h->d_left, 0, h->vbytes * (size_t)h->n * (size_t)nb, st));
+        if (kPackedColumns) {
+            CAPSP_CUDA(cudaMemsetAsync(h->d_left, 0, 2 * h->vbytes * (size_t)h->n * (size_t)nb, st));
+        } else {
+            CAPSP_CUDA(cudaMemsetAsync(h->d_arrived, 0, sizeof(int) * (size_t)h->n, st));
+            CAPSP_CUDA(cudaMemsetAsync(h->d_left, 0, h->vbytes * (size_t)h->n * (size_t)nb, st));
+        }
         CAPSP_CUDA(cudaMemsetAsync(h->d_ticket, 0, sizeof(unsigned), st));
         if (r0 == 0)
             CAPSP_CUDA(cudaMemsetAsync(h->d_err, 0, sizeof(int) * 4, st));
@@ -887,6 +898,7 @@ static capsp_status_t enqueue_cols(capsp_handle_t h, const T *b, T *x, int nrhs,
         a.order = h->d_corder[backward];
         a.arrived = h->d_arrived;
         a.left_sum = (T *)h->d_left;
+        a.slots = kPackedColumns ? h->d_left : nullptr;
         a.lsld = nb;
         a.b = b + r0;
         a.x = x + r0;
@@ -1508,6 +1520,7 @@ extern "C" capsp_status_t capsp_csc_solve_noalloc_f64(const int *colptr, const i
     a.inv_diag = inv;
     a.indeg = indeg;
     a.order = nullptr;
+    a.slots = nullptr;
     a.arrived = arrived;
     a.left_sum = left;
     a.lsld = 1;

@@ -178,6 +178,21 @@ __device__ __forceinline__ void cp_async_wait_all()
     asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
+// 16-byte compare-and-swap (gpu scope, relaxed); returns the previous value
+__device__ __forceinline__ ulonglong2 cas128(ulonglong2 *p, ulonglong2 cmp, ulonglong2 val)
+{
+    ulonglong2 r;
+    asm volatile("{\n\t.reg .b128 c, v, o;\n\t"
+                 "mov.b128 c, {%2, %3};\n\t"
+                 "mov.b128 v, {%4, %5};\n\t"
+                 "atom.relaxed.gpu.global.cas.b128 o, [%6], c, v;\n\t"
+                 "mov.b128 {%0, %1}, o;\n\t}"
+                 : "=l"(r.x), "=l"(r.y)
+                 : "l"(cmp.x), "l"(cmp.y), "l"(val.x), "l"(val.y), "l"(p)
+                 : "memory");
+    return r;
+}
+
 // Budget of one dependency wait.
 struct WaitCfg {
     unsigned long long timeout_ns;  // wall-clock budget of a single wait

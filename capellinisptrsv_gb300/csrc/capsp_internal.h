@@ -60,6 +60,8 @@ struct ColArgs {
     const int *order;  // visiting order of the columns (nullptr: index order)
     int *arrived;      // zeroed before the launch
     T *left_sum;       // zeroed before the launch, element (i, r) at i*lsld + r
+    void *slots;       // sum-and-count words instead of left_sum + arrived (nullptr: those),
+                       // zeroed before the launch; FP64 16 bytes, FP32 8 bytes per (i, r)
     long long lsld;
     const T *b;
     T *x;

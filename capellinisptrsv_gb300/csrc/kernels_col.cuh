@@ -28,6 +28,203 @@
 
 namespace capsp {
 
+// A target's partial sum and arrival count for one right-hand side, kept in one
+// atomic word: FP64 {sum bits, count} in 16 bytes, FP32 {count << 32 | sum
+// bits} in 8.  A producer's contribution is one compare-and-swap (sum + c,
+// count + 1), so the consumer that sees the full count holds the final sum in
+// the same read: no left_sum read after the wait and no fence between the
+// producer's sum and its count.
+template <typename T>
+struct SumCount;
+
+template <>
+struct SumCount<double> {
+    typedef ulonglong2 W;
+    // atomic read: a compare that never matches (no count is all ones)
+    static __device__ __forceinline__ W read(W *p)
+    {
+        return cas128(p, make_ulonglong2(0ull, ~0ull), make_ulonglong2(0ull, ~0ull));
+    }
+    // the producer's first guess of the current value (a torn read only costs a retry)
+    static __device__ __forceinline__ W guess(const W *p)
+    {
+        W r;
+        asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(r.x), "=l"(r.y) : "l"(p));
+        return r;
+    }
+    static __device__ __forceinline__ double sum(W w) { return __longlong_as_double((long long)w.x); }
+    static __device__ __forceinline__ unsigned long long count(W w) { return w.y; }
+    static __device__ __forceinline__ W add(W w, double c)
+    {
+        return make_ulonglong2((unsigned long long)__double_as_longlong(sum(w) + c), w.y + 1ull);
+    }
+    static __device__ __forceinline__ bool same(W a, W b) { return a.x == b.x && a.y == b.y; }
+    static __device__ __forceinline__ W cas(W *p, W cmp, W val) { return cas128(p, cmp, val); }
+};
+
+template <>
+struct SumCount<float> {
+    typedef unsigned long long W;
+    static __device__ __forceinline__ W read(W *p) { return ld_relaxed(p); }  // 8-byte single-copy atomic
+    static __device__ __forceinline__ W guess(const W *p) { return ld_relaxed(p); }
+    static __device__ __forceinline__ float sum(W w) { return __uint_as_float((unsigned)(w & 0xffffffffull)); }
+    static __device__ __forceinline__ unsigned long long count(W w) { return w >> 32; }
+    static __device__ __forceinline__ W add(W w, float c)
+    {
+        return ((count(w) + 1ull) << 32) | (unsigned long long)__float_as_uint(sum(w) + c);
+    }
+    static __device__ __forceinline__ bool same(W a, W b) { return a == b; }
+    static __device__ __forceinline__ W cas(W *p, W cmp, W val) { return atomicCAS(p, cmp, val); }
+};
+
+// Column-driven solve on sum-and-count words (a.slots, zeroed before the
+// launch, word (i, r) at i*lsld + r): the same schedule, waits and fused
+// gradient as col_solve_kernel below.  A failed compare-and-swap means another
+// producer of the same target succeeded, so a producer retries at most as
+// often as the target has producers; kCasRetries only backstops that bound.
+constexpr int kCasPasses = 4;  // entry passes whose guesses are fetched before the wait
+constexpr int kCasRetries = 1 << 20;
+
+template <typename T, int G>
+__global__ void __launch_bounds__(512) col_solve_packed_kernel(const ColArgs<T> a)
+{
+    typedef VBits<T> VB;
+    typedef SumCount<T> SC;
+    typedef typename SC::W W;
+    constexpr int EPW = 32 / G;
+    const int lane = threadIdx.x & 31;
+    const int es = lane / G, g = lane % G;
+    const bool active = g < a.nrhs;
+    W *slots = reinterpret_cast<W *>(a.slots);
+    for (;;) {
+        unsigned tk = 0, stop = 0;
+        if (lane == 0) {
+            tk = atomicAdd(a.ticket, 1u);
+            stop = ld_relaxed(reinterpret_cast<const unsigned *>(a.err));
+        }
+        tk = __shfl_sync(kFullMask, tk, 0);
+        stop = __shfl_sync(kFullMask, stop, 0);
+        if (stop || tk >= (unsigned)a.n)
+            break;
+        const int j = a.order != nullptr ? __ldg(a.order + tk) : (a.backward ? a.n - 1 - (int)tk : (int)tk);
+        const int s0 = __ldg(a.ptr + j), e0 = __ldg(a.ptr + j + 1);
+        const int s = a.backward ? s0 : s0 + 1;
+        const int e = a.backward ? e0 - 1 : e0;
+        const int need = __ldg(a.indeg + j) - 1;
+        const T dinv = __ldg(a.inv_diag + j);
+        // before the wait: the first passes of entries, each target word's
+        // current value as the compare-and-swap guess, and the fused gradient's
+        // first x value
+        int rr[kCasPasses];
+        T vv[kCasPasses];
+        W gw[kCasPasses];
+#pragma unroll
+        for (int q = 0; q < kCasPasses; ++q) {
+            const int k = s + es + q * EPW;
+            rr[q] = 0;
+            vv[q] = T(0);
+            gw[q] = W();
+            if (k < e) {
+                rr[q] = __ldg(a.idx + k);
+                vv[q] = __ldg(a.val + k);
+                if (active)
+                    gw[q] = SC::guess(slots + (size_t)rr[q] * (size_t)a.lsld + g);
+            }
+        }
+        const int kg1 = s0 + es;
+        T xg1 = T(0);
+        if (a.grad_val != nullptr && kg1 < e0 && active)
+            xg1 = __ldg(a.xf + (size_t)__ldg(a.idx + kg1) * (size_t)a.ld + g);
+        bool aborted = false;
+        T xj = T(0);
+        if (es == 0 && active) {
+            const size_t xo = (size_t)j * (size_t)a.ld + g;
+            const T bj = __ldg(a.b + xo);
+            T ls = T(0);
+            if (need > 0) {
+                W *mine = slots + (size_t)j * (size_t)a.lsld + g;
+                Spin sp;
+                W w = SC::read(mine);
+                while (SC::count(w) != (unsigned long long)need) {
+                    if (sp.next(a.err, a.wait, j, j)) {
+                        aborted = true;
+                        break;
+                    }
+                    w = SC::read(mine);
+                }
+                ls = SC::sum(w);
+            }
+            xj = aborted ? VB::from(VB::kQNaN) : (bj - ls) * dinv;
+            a.x[xo] = xj;
+        }
+        xj = __shfl_sync(kFullMask, xj, g);
+        if (j != a.stuck_row && active) {
+            // all prefetched passes' compare-and-swaps in flight together,
+            // then the (rare) retries
+            W got[kCasPasses];
+#pragma unroll
+            for (int q = 0; q < kCasPasses; ++q) {
+                got[q] = W();
+                if (s + es + q * EPW < e)
+                    got[q] = SC::cas(slots + (size_t)rr[q] * (size_t)a.lsld + g, gw[q], SC::add(gw[q], xj * vv[q]));
+            }
+#pragma unroll
+            for (int q = 0; q < kCasPasses; ++q) {
+                if (s + es + q * EPW < e && !SC::same(got[q], gw[q])) {
+                    W *p = slots + (size_t)rr[q] * (size_t)a.lsld + g;
+                    W old = got[q];
+                    for (int it = 0;; ++it) {
+                        const W now = SC::cas(p, old, SC::add(old, xj * vv[q]));
+                        if (SC::same(now, old))
+                            break;
+                        old = now;
+                        if (it > kCasRetries) {
+                            if (atomicCAS(a.err + kErrStatus, 0, kStatusTimeout) == 0) {
+                                a.err[kErrRow] = rr[q];
+                                a.err[kErrWaitedOn] = j;
+                            }
+                            break;
+                        }
+                    }
+                }
+            }
+            // passes beyond the prefetched ones: guess, then compare-and-swap
+            for (int k = s + es + kCasPasses * EPW; k < e; k += EPW) {
+                W *p = slots + (size_t)__ldg(a.idx + k) * (size_t)a.lsld + g;
+                const T c = xj * __ldg(a.val + k);
+                W old = SC::guess(p);
+                for (int it = 0;; ++it) {
+                    const W now = SC::cas(p, old, SC::add(old, c));
+                    if (SC::same(now, old))
+                        break;
+                    old = now;
+                    if (it > kCasRetries) {
+                        if (atomicCAS(a.err + kErrStatus, 0, kStatusTimeout) == 0) {
+                            a.err[kErrRow] = (int)(p - slots) / (int)a.lsld;
+                            a.err[kErrWaitedOn] = j;
+                        }
+                        break;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (a.grad_val != nullptr) {
+            for (int kb = s0; kb < e0; kb += EPW) {
+                const int k = kb + es;
+                T prod = T(0);
+                if (k < e0 && active)
+                    prod = xj * (k == kg1 ? xg1 : __ldg(a.xf + (size_t)__ldg(a.idx + k) * (size_t)a.ld + g));
+#pragma unroll
+                for (int off = G / 2; off >= 1; off >>= 1)
+                    prod += __shfl_xor_sync(kFullMask, prod, off);
+                if (k < e0 && g == 0)
+                    a.grad_val[k] = a.grad_accumulate ? a.grad_val[k] - prod : -prod;
+            }
+        }
+    }
+}
+
 template <typename T, int G>
 __global__ void __launch_bounds__(512) col_solve_kernel(const ColArgs<T> a)
 {
@@ -119,7 +316,7 @@ template <typename T, int G>
 static cudaError_t launch_col_impl(const ColArgs<T> &a, int block, int bps, int num_sms,
                                    cudaStream_t st)
 {
-    auto kern = col_solve_kernel<T, G>;
+    auto kern = a.slots != nullptr ? col_solve_packed_kernel<T, G> : col_solve_kernel<T, G>;
     int occ = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, block, 0);
     if (e != cudaSuccess)
