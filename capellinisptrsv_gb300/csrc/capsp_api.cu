@@ -917,10 +917,13 @@ static capsp_status_t enqueue_cols(capsp_handle_t h, const T *b, T *x, int nrhs,
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k0, st));
         // default launch shape of the column path (measured on GB300): a warp
-        // holds one column, so wide levels want every warp an SM can hold,
-        // narrow ones two 256-thread blocks per SM
-        const int cblock = tn.dflt ? 256 : tn.block;
-        const int cbps = tn.dflt ? (h->col_narrow[backward] ? 2 : 0) : tn.bps;
+        // holds one column, so wide levels want every warp an SM can hold;
+        // narrow ones three blocks per SM, of 256 threads with one right-hand
+        // side and of 128 with several (grad_1m transpose + grad: 1.69 -> 1.53
+        // ms at 1 RHS, 4.26 -> 4.09 ms at 16 RHS, against two blocks of 256)
+        const bool cnarrow = h->col_narrow[backward];
+        const int cblock = tn.dflt ? (cnarrow && nb > 1 ? 128 : 256) : tn.block;
+        const int cbps = tn.dflt ? (cnarrow ? 3 : 0) : tn.bps;
         CAPSP_CUDA(launch_col_solve<T>(a, cblock, cbps, h->num_sms, st));
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k1, st));
@@ -1170,7 +1173,7 @@ extern "C" capsp_status_t capsp_autotune(capsp_handle_t h, const void *b, void *
     } else {
         cands.push_back({kRowWrtFst, 1, 256, 0, h->border, true});  // the default shape
         for (int bl : blocks)
-            for (int bp : {0, 2})
+            for (int bp : {0, 2, 3, 4})
                 cands.push_back({kRowWrtFst, 1, bl, bp, h->border});
     }
     cudaEvent_t e0, e1;
