@@ -79,7 +79,7 @@ typedef enum capsp_algorithm {
     CAPSP_ALG_WRTFST = 1,      /* thread per row, write-first (CUDA/ourWrtFst) */
     CAPSP_ALG_TWOPART = 2,     /* thread per row, out-of-warp then in-warp phases (CUDA/our2Part) */
     CAPSP_ALG_MIX = 3,         /* thread or warp per row by nnz/row of 32-row groups (CUDA/mix) */
-    CAPSP_ALG_SYNCFREE_CSC = 4 /* warp per column with left_sum atomics (CUDA/SyncFree_csc) */
+    CAPSP_ALG_SYNCFREE_CSC = 4 /* warp per column, atomic partial sums + arrival counts (CUDA/SyncFree_csc) */
 } capsp_algorithm_t;
 
 /* Order in which the row-driven kernels start rows.  Any order that lists a
