@@ -82,7 +82,10 @@ struct SumCount<float> {
 // gradient as col_solve_kernel below.  A failed compare-and-swap means another
 // producer of the same target succeeded, so a producer retries at most as
 // often as the target has producers; kCasRetries only backstops that bound.
-constexpr int kCasPasses = 4;  // entry passes whose guesses are fetched before the wait
+// entry passes whose guesses are fetched before the wait: enough for columns of
+// 8 entries or more at every width (one pass covers 32/G entries), no more, so
+// the narrow builds keep their registers (1 RHS: 1.54 -> 1.48 ms on grad_1m)
+constexpr int kCasPassesMax = 4;
 constexpr int kCasRetries = 1 << 20;
 
 template <typename T, int G>
@@ -92,6 +95,7 @@ __global__ void __launch_bounds__(512) col_solve_packed_kernel(const ColArgs<T> 
     typedef SumCount<T> SC;
     typedef typename SC::W W;
     constexpr int EPW = 32 / G;
+    constexpr int kCasPasses = G >= 8 ? kCasPassesMax : (G >= 2 ? 2 : 1);
     const int lane = threadIdx.x & 31;
     const int es = lane / G, g = lane % G;
     const bool active = g < a.nrhs;
