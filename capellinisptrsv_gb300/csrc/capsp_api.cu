@@ -916,14 +916,18 @@ static capsp_status_t enqueue_cols(capsp_handle_t h, const T *b, T *x, int nrhs,
         const bool prof = h->profiling && r0 == 0;
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k0, st));
-        // default launch shape of the column path (measured on GB300): a warp
-        // holds one column, so wide levels want every warp an SM can hold;
-        // narrow ones three blocks per SM, of 256 threads with one right-hand
-        // side and of 128 with several (grad_1m transpose + grad: 1.69 -> 1.53
-        // ms at 1 RHS, 4.26 -> 4.09 ms at 16 RHS, against two blocks of 256)
+        // default launch shape of the column path (measured on GB300, one warp
+        // per column): three blocks per SM.  Narrow levels take 128-thread
+        // blocks, except a single right-hand side with the fused gradient,
+        // whose longer per-column work wants 256 (grad_1m transpose + grad:
+        // 1.69 -> 1.53 ms at 1 RHS, 4.26 -> 4.09 ms at 16 RHS, against two
+        // blocks of 256; CSC forward 2.01 -> 1.87 ms).  Wide levels take
+        // 256-thread blocks with one right-hand side (wide_4m CSC forward 4.94
+        // -> 4.11 ms against every resident warp) and every resident warp
+        // with several.
         const bool cnarrow = h->col_narrow[backward];
-        const int cblock = tn.dflt ? (cnarrow && nb > 1 ? 128 : 256) : tn.block;
-        const int cbps = tn.dflt ? (cnarrow ? 3 : 0) : tn.bps;
+        const int cblock = tn.dflt ? (cnarrow && (nb > 1 || grad == nullptr) ? 128 : 256) : tn.block;
+        const int cbps = tn.dflt ? ((cnarrow || nb == 1) ? 3 : 0) : tn.bps;
         CAPSP_CUDA(launch_col_solve<T>(a, cblock, cbps, h->num_sms, st));
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k1, st));
