@@ -244,7 +244,8 @@ def run_reference_forms(args):
     sec = statistics.mean(t)
     value = per_step / sec if per_step else sec * 1e3
     line = {
-        "impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": 0, "steps": steps,
+        "impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": args.gpus, "gpus_used": 0,
+        "steps": steps,
         "warmup": min(args.warmup, 3), "ms_per_step": sec * 1e3, "higher_is_better": hib, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, seed 0)",
         "config": {"workload": args.workload, "rhs": k},
@@ -278,7 +279,7 @@ def run_reference(args):
     val_gf = flops / sec / 1e9
     line = {
         "impl": "reference", "metric": "SpTRSV GFLOP/s (2*nnz-n flops per solve)", "value": val_gf,
-        "unit": "GFLOP/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "unit": "GFLOP/s", "n_gpus": args.gpus, "gpus_used": 0, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": args.dtype, "data": "synthetic (seeded generator, seed 0)",
         "config": {"workload": args.workload, "n": m.n, "nnz": m.nnz, "rhs": 1,
