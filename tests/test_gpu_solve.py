@@ -145,6 +145,25 @@ def test_multi_rhs_forward_adjoint_grad(nrhs, schedule):
     assert rel_inf_err(host(gv2), go) <= TOL64
 
 
+@pytest.mark.parametrize("nrhs", [1, 4, 16])
+def test_f32_forward_adjoint_grad(nrhs):
+    """FP32 through the column kernel's 8-byte sum-and-count words, against the FP64 oracle."""
+    m = cs.generate(n=30_000, kmin=1, kmax=9, band=3000, seed=60 + nrhs)
+    shape = (m.n, nrhs) if nrhs > 1 else (m.n,)
+    b = np.random.default_rng(nrhs).standard_normal(shape)
+    g = np.random.default_rng(nrhs + 100).standard_normal(shape)
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
+    yo = oracle.solve_csr_transpose(m.rowptr, m.colidx, m.val, g)
+    go = oracle.grad_val(m.rowptr, m.colidx, yo, xo)
+    s = solver_for(m, np.float32)
+    x = s.solve(dev(b.astype(np.float32)))
+    y, gv = s.solve_transpose_grad(dev(g.astype(np.float32)), x)
+    s.status()
+    assert rel_inf_err(host(x), xo) <= TOL32
+    assert rel_inf_err(host(y), yo) <= TOL32
+    assert rel_inf_err(host(gv), go) <= TOL32
+
+
 @pytest.mark.parametrize("schedule", SCHEDULES)
 def test_strided_rhs_layout(schedule):
     """ld > nrhs: a column slice of a wider buffer."""
