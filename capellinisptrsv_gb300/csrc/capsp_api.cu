@@ -922,12 +922,11 @@ static capsp_status_t enqueue_cols(capsp_handle_t h, const T *b, T *x, int nrhs,
         // whose longer per-column work wants 256 (grad_1m transpose + grad:
         // 1.69 -> 1.53 ms at 1 RHS, 4.26 -> 4.09 ms at 16 RHS, against two
         // blocks of 256; CSC forward 2.01 -> 1.87 ms).  Wide levels take
-        // 256-thread blocks with one right-hand side (wide_4m CSC forward 4.94
-        // -> 4.11 ms against every resident warp) and every resident warp
-        // with several.
+        // 256-thread blocks (wide_4m CSC forward 4.94 -> 4.11 ms, transpose
+        // with 4 RHS 3.98 -> 3.59 ms, against every resident warp).
         const bool cnarrow = h->col_narrow[backward];
         const int cblock = tn.dflt ? (cnarrow && (nb > 1 || grad == nullptr) ? 128 : 256) : tn.block;
-        const int cbps = tn.dflt ? ((cnarrow || nb == 1) ? 3 : 0) : tn.bps;
+        const int cbps = tn.dflt ? 3 : tn.bps;
         CAPSP_CUDA(launch_col_solve<T>(a, cblock, cbps, h->num_sms, st));
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k1, st));
