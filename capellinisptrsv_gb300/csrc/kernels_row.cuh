@@ -157,6 +157,19 @@ __host__ __device__ constexpr size_t warp_smem_bytes(int R, int RPL = 1, bool st
            (stage ? (size_t)kStage * (sizeof(int) + sizeof(T)) : 0);
 }
 
+// The 16-byte staging copies need every warp's block, and the staging buffers
+// inside it (after the mirror and slot parts; positions, then kStage values
+// later), to start on a 16-byte boundary.
+template <typename T>
+__host__ __device__ constexpr bool staging_aligned()
+{
+    return warp_smem_bytes<T>(1, 1, true) % 16 == 0 && warp_smem_bytes<T>(2, 1, true) % 16 == 0 &&
+           warp_smem_bytes<T>(4, 1, true) % 16 == 0 && warp_smem_bytes<T>(1, 1, false) % 16 == 0 &&
+           warp_smem_bytes<T>(2, 1, false) % 16 == 0 && warp_smem_bytes<T>(4, 1, false) % 16 == 0 &&
+           warp_smem_bytes<T>(1, 4, false) % 16 == 0 && (kStage * sizeof(int)) % 16 == 0;
+}
+static_assert(staging_aligned<double>() && staging_aligned<float>(), "shared-memory parts must be 16-byte multiples");
+
 // Convergent chunk solve.  The warp's chunk holds schedule positions
 // [lo, lo + CH); in each pass over a sub-chunk of 32/G positions starting at
 // `sub`, lane (rl, g) owns the element (position p = sub + rl, rhs g).  All
