@@ -37,7 +37,7 @@ class Info(C.Structure):
                 ("warp_occupy", C.c_double), ("element_occupy", C.c_double),
                 ("analyse_ms", C.c_double), ("rows_per_thread", C.c_int),
                 ("block_threads", C.c_int), ("blocks_per_sm", C.c_int), ("num_sms", C.c_int),
-                ("schedule", C.c_int), ("levels", C.c_int)]
+                ("schedule", C.c_int), ("levels", C.c_int), ("cached_graphs", C.c_int)]
 
 
 class GenParams(C.Structure):

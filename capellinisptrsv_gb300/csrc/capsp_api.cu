@@ -4,6 +4,7 @@
 // capsp_set_values, capsp_status_sync, capsp_solve_host and capsp_autotune.
 #include "capsp.h"
 #include "capsp_internal.h"
+#include "graph_cache.h"
 
 #include <chrono>
 #include <climits>
@@ -75,7 +76,8 @@ struct MixTable {
     double wo = 0.0, eo = 0.0;
 };
 
-typedef std::tuple<const void *, void *, int, int64_t, void *, int> GraphKey;
+void destroy_graph_exec(cudaGraphExec_t e) { cudaGraphExecDestroy(e); }
+typedef GraphCache<cudaGraphExec_t, destroy_graph_exec> Graphs;
 
 struct DeviceGuard {
     int prev = -1;
@@ -132,7 +134,7 @@ struct capsp_handle_s {
     // 7 % faster on deep chains (zipf_1m), where it delays each detection
     WaitCfg wait = {10000000000ull, 1u << 30, 0u};
     int stuck_row = -1;
-    std::map<GraphKey, cudaGraphExec_t> graphs;
+    Graphs graphs;  // capsp_graph_solve; invalidated by every change a capture bakes in
     void *d_stage = nullptr;
     size_t stage_bytes = 0;
     cudaStream_t stage_stream = nullptr;
@@ -161,8 +163,7 @@ static void free_handle(capsp_handle_t h)
     if (!h)
         return;
     DeviceGuard g(h->device);
-    for (auto &kv : h->graphs)
-        cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
     for (auto &kv : h->mix)
         cudaFree(kv.second.d);
     if (h->own_struct) {
@@ -250,6 +251,7 @@ static capsp_status_t build_level(capsp_handle_t h)
 {
     if (h->level_built)
         return CAPSP_OK;
+    h->graphs.invalidate();
     const int n = h->n, nnz = h->nnz;
     const int upper = row_view_upper(h);
     std::vector<int> idx((size_t)nnz);
@@ -469,6 +471,7 @@ extern "C" capsp_status_t capsp_set_values(capsp_handle_t h, const void *val)
         return fail(CAPSP_ERR_INVALID, "handle and val must be non-NULL");
     std::lock_guard<std::recursive_mutex> lk(h->mu);
     DeviceGuard g(h->device);
+    h->graphs.invalidate();  // captured natural-schedule solves read d_val directly
     if (h->flags & CAPSP_DEVICE_POINTERS) {
         h->d_val = const_cast<void *>(val);
     } else {
@@ -491,8 +494,10 @@ extern "C" capsp_status_t capsp_refresh_values(capsp_handle_t h, const void *val
                     "capsp_refresh_values needs a CAPSP_DEVICE_POINTERS handle; use capsp_set_values");
     std::lock_guard<std::recursive_mutex> lk(h->mu);
     DeviceGuard g(h->device);
-    if (val)
+    if (val && val != h->d_val) {
+        h->graphs.invalidate();
         h->d_val = const_cast<void *>(val);
+    }
     const int dl = diag_last_of(h->format, h->uplo);
     cudaStream_t st = (cudaStream_t)stream;
     int *bad = h->d_err + 3;  // sticky diagnostic slot: first row with a bad diagonal
@@ -513,6 +518,7 @@ extern "C" capsp_status_t capsp_set_schedule(capsp_handle_t h, int schedule)
     DeviceGuard g(h->device);
     h->sched = schedule;
     h->tuned.clear();
+    h->graphs.invalidate();
     if (schedule == CAPSP_SCHED_LEVEL)
         return build_level(h);
     return CAPSP_OK;
@@ -524,6 +530,7 @@ extern "C" capsp_status_t capsp_set_backoff(capsp_handle_t h, unsigned sleep_max
         return fail(CAPSP_ERR_INVALID, "handle is NULL");
     std::lock_guard<std::recursive_mutex> lk(h->mu);
     h->wait.sleep_max_ns = sleep_max_ns;
+    h->graphs.invalidate();
     return CAPSP_OK;
 }
 
@@ -540,6 +547,7 @@ extern "C" capsp_status_t capsp_set_algorithm(capsp_handle_t h, int algorithm)
     std::lock_guard<std::recursive_mutex> lk(h->mu);
     h->alg = algorithm;
     h->tuned.clear();
+    h->graphs.invalidate();
     return CAPSP_OK;
 }
 
@@ -552,6 +560,7 @@ extern "C" capsp_status_t capsp_set_mix_border(capsp_handle_t h, int border)
     h->tune.border = border;
     h->border_explicit = true;
     h->tuned.clear();
+    h->graphs.invalidate();
     return CAPSP_OK;
 }
 
@@ -572,6 +581,7 @@ extern "C" capsp_status_t capsp_set_tuning(capsp_handle_t h, int rows_per_thread
     h->tune.bps = blocks_per_sm;
     h->tune_explicit = true;
     h->tuned.clear();
+    h->graphs.invalidate();
     return CAPSP_OK;
 }
 
@@ -581,6 +591,7 @@ extern "C" capsp_status_t capsp_set_timeout(capsp_handle_t h, uint64_t timeout_n
         return fail(CAPSP_ERR_INVALID, "need a handle and a positive timeout");
     std::lock_guard<std::recursive_mutex> lk(h->mu);
     h->wait.timeout_ns = timeout_ns;
+    h->graphs.invalidate();
     return CAPSP_OK;
 }
 
@@ -592,6 +603,7 @@ extern "C" capsp_status_t capsp_debug_set_stuck_row(capsp_handle_t h, int row, u
     h->stuck_row = row;
     if (timeout_ns)
         h->wait.timeout_ns = timeout_ns;
+    h->graphs.invalidate();
     return CAPSP_OK;
 }
 
@@ -611,6 +623,7 @@ static capsp_status_t ensure_mix(capsp_handle_t h, int group_rows, int border, M
     const bool level = h->sched == CAPSP_SCHED_LEVEL;
     MixTable &mt = h->mix[group_rows * 2 + (level ? 1 : 0)];
     if (mt.d == nullptr || mt.border != border) {
+        h->graphs.invalidate();  // a captured launch holds the old table's length
         std::vector<int> table((size_t)h->n + 2);
         double wo = 0.0, eo = 0.0;
         const int len = level ? capsp_mix_table(h->n, h->h_lcum.data(), 0, group_rows, border, table.data(),
@@ -646,6 +659,7 @@ static capsp_status_t ensure_column_scratch(capsp_handle_t h, int nrhs)
         CAPSP_CUDA(cudaMalloc(&h->d_arrived, sizeof(int) * (size_t)h->n));
     const int want = nrhs < 32 ? nrhs : 32;
     if (h->left_cap < want) {
+        h->graphs.invalidate();  // captured column solves point at the old words
         cudaFree(h->d_left);
         h->d_left = nullptr;
         h->left_cap = 0;
@@ -784,6 +798,7 @@ static capsp_status_t ensure_xp(capsp_handle_t h, int nrhs)
 {
     const int want = nrhs < 32 ? nrhs : 32;
     if (h->xp_cap < want) {
+        h->graphs.invalidate();  // captured row solves point at the old scratch
         cudaFree(h->d_xp);
         h->d_xp = nullptr;
         h->xp_cap = 0;
@@ -1050,6 +1065,9 @@ static capsp_status_t prepare(capsp_handle_t h, int nrhs, bool transpose)
         }
         return CAPSP_OK;
     }
+    // column path: CSC solve (forward for lower) or CSR transpose (backward for lower)
+    const int backward = transpose ? (h->uplo == CAPSP_LOWER) : (h->uplo == CAPSP_UPPER);
+    CAPSP_TRY(ensure_column_order(h, backward));
     return ensure_column_scratch(h, nrhs);
 }
 
@@ -1082,15 +1100,19 @@ extern "C" capsp_status_t capsp_status_sync(capsp_handle_t h, void *stream)
     return CAPSP_OK;
 }
 
-// Device address of page-locked host memory (nullptr for pageable or device memory).
-static void *pinned_alias(const void *p)
+// Device address, on `device`, of page-locked host memory (nullptr for
+// pageable or device memory, and for memory page-locked in another device's
+// context, which need not be mapped for this one).
+static void *pinned_alias(const void *p, int device)
 {
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
-    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+    if (at.type != cudaMemoryTypeHost || at.device != device)
+        return nullptr;
+    return at.devicePointer;
 }
 
 extern "C" capsp_status_t capsp_solve_host(capsp_handle_t h, const void *b_host, void *x_host, int nrhs)
@@ -1122,7 +1144,7 @@ extern "C" capsp_status_t capsp_solve_host(capsp_handle_t h, const void *b_host,
     // 4 right-hand sides, 32 bytes per read, 8.97 ms in place, 11.2 copied).
     void *b_in_place = (h->format == CAPSP_FMT_CSR && h->sched == CAPSP_SCHED_LEVEL &&
                         !(wide_levels(h) && nrhs == 1))
-                           ? pinned_alias(b_host)
+                           ? pinned_alias(b_host, h->device)
                            : nullptr;
     if (b_in_place) {
         CAPSP_TRY(dispatch(h, kOpSolve, b_in_place, dx, nullptr, nullptr, nrhs, nrhs, st));
@@ -1228,6 +1250,7 @@ extern "C" capsp_status_t capsp_autotune(capsp_handle_t h, const void *b, void *
     CAPSP_TRY(st_all);
     CAPSP_TRY(capsp_status_sync(h, stream));
     h->tuned[nrhs] = best_t;
+    h->graphs.invalidate();
     if (best_ms)
         *best_ms = best;
     return CAPSP_OK;
@@ -1247,11 +1270,14 @@ extern "C" capsp_status_t capsp_graph_solve(capsp_handle_t h, const void *b, voi
     std::lock_guard<std::recursive_mutex> lk(h->mu);
     DeviceGuard g(h->device);
     cudaStream_t st = (cudaStream_t)stream;
+    // scratch first: a reallocation here invalidates the cache, so the key
+    // below carries the generation the capture will be valid for
+    CAPSP_TRY(prepare(h, nrhs, false));
     const Tuning tn = current_tuning(h, nrhs);
-    const GraphKey key(b, x, nrhs, ld, stream, tn.kind * 1000003 + tn.R * 10007 + tn.block * 101 + tn.border);
-    auto it = h->graphs.find(key);
-    if (it == h->graphs.end()) {
-        CAPSP_TRY(prepare(h, nrhs, false));
+    const GraphKey key = {b, x, nrhs, ld, stream, tn.kind, tn.R, tn.block, tn.bps, tn.border, tn.dflt ? 1 : 0,
+                          h->graphs.generation()};
+    cudaGraphExec_t *exec_p = h->graphs.find(key);
+    if (!exec_p) {
         CAPSP_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         capsp_status_t s = dispatch(h, kOpSolve, b, x, nullptr, nullptr, nrhs, ld, st);
         cudaGraph_t graph = nullptr;
@@ -1268,9 +1294,12 @@ extern "C" capsp_status_t capsp_graph_solve(capsp_handle_t h, const void *b, voi
         cudaGraphDestroy(graph);
         if (e != cudaSuccess)
             return fail(CAPSP_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
-        it = h->graphs.emplace(key, exec).first;
+        // the capture must not have changed what it depends on (prepare() ran first)
+        if (!h->graphs.put(key, exec))
+            return fail(CAPSP_ERR_CUDA, "scratch changed during graph capture");
+        exec_p = h->graphs.find(key);
     }
-    CAPSP_CUDA(cudaGraphLaunch(it->second, st));
+    CAPSP_CUDA(cudaGraphLaunch(*exec_p, st));
     return CAPSP_OK;
 }
 
@@ -1288,6 +1317,8 @@ extern "C" capsp_status_t capsp_set_profiling(capsp_handle_t h, int enable)
         CAPSP_CUDA(cudaEventCreate(&h->ev_k0));
         CAPSP_CUDA(cudaEventCreate(&h->ev_k1));
     }
+    if (h->profiling != (enable != 0))
+        h->graphs.invalidate();  // captures record the timing events only while profiling
     h->profiling = enable != 0;
     return CAPSP_OK;
 }
@@ -1298,6 +1329,7 @@ extern "C" capsp_status_t capsp_debug_trace(capsp_handle_t h, void *row_times_ns
         return fail(CAPSP_ERR_INVALID, "handle is NULL");
     std::lock_guard<std::recursive_mutex> lk(h->mu);
     h->trace = (unsigned long long *)row_times_ns;
+    h->graphs.invalidate();
     return CAPSP_OK;
 }
 
@@ -1339,6 +1371,7 @@ extern "C" capsp_status_t capsp_get_info(capsp_handle_t h, capsp_info_t *info)
     info->blocks_per_sm = bps;
     info->schedule = h->sched;
     info->levels = h->levels;
+    info->cached_graphs = (int)h->graphs.size();
     if (h->format == CAPSP_FMT_CSC) {
         info->algorithm = CAPSP_ALG_SYNCFREE_CSC;
     } else {
@@ -1452,10 +1485,8 @@ constexpr size_t kNoallocLeft = kNoallocInv + sizeof(double) * kNoallocMaxN;
 constexpr size_t kNoallocIndeg = kNoallocLeft + sizeof(double) * kNoallocMaxN;
 constexpr size_t kNoallocArrived = kNoallocIndeg + sizeof(int) * kNoallocMaxN;
 constexpr size_t kNoallocBytes = kNoallocArrived + sizeof(int) * kNoallocMaxN;
-constexpr int kNoallocMaxDevices = 64;
 
 std::mutex g_noalloc_mu;
-void *g_noalloc_base[kNoallocMaxDevices] = {};
 
 }  // namespace
 
@@ -1479,19 +1510,20 @@ extern "C" capsp_status_t capsp_csc_solve_noalloc_f64(const int *colptr, const i
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     int dev = 0, sms = 0;
     CAPSP_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kNoallocMaxDevices)
-        return fail(CAPSP_ERR_UNSUPPORTED, "device ordinal %d is beyond %d", dev, kNoallocMaxDevices);
-    if (!g_noalloc_base[dev]) {
-        // first call on this device: resolve the scratch address with the device current
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p)
+    // The scratch's device address, resolved with the caller's device current
+    // on every call: g_noalloc_scratch names a host-side stand-in in host
+    // code, and the address can change when the caller resets the device
+    // (the module is loaded again into the new context).  The lookup
+    // allocates nothing and costs far less than the call's two synchronisations.
+    void *scratch = nullptr;
+    {
+        const cudaError_t e = cudaGetSymbolAddress(&scratch, g_noalloc_scratch);
+        if (e != cudaSuccess || !scratch)
             return fail(CAPSP_ERR_CUDA, "cudaGetSymbolAddress of the static scratch failed: %s",
                         cudaGetErrorString(e));
-        g_noalloc_base[dev] = p;
     }
     CAPSP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    unsigned char *base = static_cast<unsigned char *>(g_noalloc_base[dev]);
+    unsigned char *base = static_cast<unsigned char *>(scratch);
     unsigned *ticket = reinterpret_cast<unsigned *>(base);
     int *err = reinterpret_cast<int *>(base + 16);
     int *bad = reinterpret_cast<int *>(base + 32);
@@ -1511,8 +1543,8 @@ extern "C" capsp_status_t capsp_csc_solve_noalloc_f64(const int *colptr, const i
     CAPSP_CUDA(cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
     CAPSP_CUDA(cudaStreamSynchronize(st));
     if (h_bad < n)
-        return fail(CAPSP_ERR_INVALID, "column %d is malformed (lower CSC needs the diagonal first, "
-                                       "rows ascending and below it)", h_bad);
+        return fail(CAPSP_ERR_INVALID, "column %d is malformed (lower CSC needs the diagonal first and "
+                                       "every other row index below it and below n)", h_bad);
 
     CAPSP_CUDA(cudaMemsetAsync(left, 0, sizeof(double) * nn, st));
     CAPSP_CUDA(cudaMemsetAsync(indeg, 0, sizeof(int) * nn, st));

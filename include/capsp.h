@@ -113,6 +113,9 @@ typedef struct capsp_info {
     int num_sms;
     int schedule;           /* capsp_schedule_t of the row-driven kernels */
     int levels;             /* dependency levels (0 until a level schedule was built) */
+    int cached_graphs;      /* instantiated graphs held for capsp_graph_solve; every change that a
+                               captured solve depends on (scratch growth, new value pointer,
+                               schedule, tuning, wait budget, debug hooks) drops them all */
 } capsp_info_t;
 
 /* ------------------------------------------------------------------------ */
@@ -275,13 +278,13 @@ capsp_status_t capsp_hop_latency(int n, int stride, int dtype, float *ns_per_hop
  * one static device array of 1.5 MiB, sized for at most 65,536 rows, that
  * every GPU which loads the library holds until the process exits; a larger
  * n is rejected with CAPSP_ERR_INVALID.  All pointers are device pointers;
- * colptr/rowidx must hold the diagonal first in each column (checked on the
- * device before the solve).  The call resets every scratch part that must
+ * colptr/rowidx must hold the diagonal first in each column and every other
+ * row index below it and below n (checked on the device before the solve).  The call resets every scratch part that must
  * start at zero itself, then synchronises `stream` and returns the solve's
- * status.  The first call on a device resolves the scratch address
- * (cudaGetSymbolAddress, with that device current) and must come before any
- * stream capture.  All calls share the scratch, so overlapping calls would
- * race on it: a process-wide lock serialises them. */
+ * status: it is synchronous.  Every call resolves the scratch's device address
+ * (cudaGetSymbolAddress, with the caller's device current), so a device reset
+ * by the caller is picked up.  All calls share the scratch, so overlapping
+ * calls would race on it: a process-wide lock serialises them. */
 capsp_status_t capsp_csc_solve_noalloc_f64(const int *colptr, const int *rowidx, const double *val,
                                            int n, int nnz, const double *b, double *x, void *stream);
 

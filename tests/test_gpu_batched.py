@@ -68,3 +68,58 @@ def test_batched_rejects_cross_system_entries():
     ci[m.rowptr[r]:m.rowptr[r + 1] - 1].sort()
     with pytest.raises(cs.CapspError):
         cs.TriangularSolver(m.rowptr, ci, m.val, sys_rowoff=m.sys_rowoff)
+
+
+def test_graph_cache_after_scratch_growth(batch):
+    """Graph-solve with 4 RHS, plain-solve with 16 (the handle's scratch grows
+    and the memory the first capture points at is freed), graph-solve with 4
+    again: the cache must have dropped the stale graph and recaptured."""
+    m = batch
+    rng = np.random.default_rng(21)
+    b4 = rng.standard_normal((m.n, 4))
+    b16 = rng.standard_normal((m.n, 16))
+    s = cs.TriangularSolver(t(m.rowptr), t(m.colidx), t(m.val), sys_rowoff=m.sys_rowoff)
+    st = torch.cuda.Stream()
+    b4d, x4 = t(b4), torch.empty((m.n, 4), dtype=torch.float64, device=DEV)
+    with torch.cuda.stream(st):
+        s.graph_solve(b4d, x4, st)
+    st.synchronize()
+    assert s.info()["cached_graphs"] == 1
+    x16 = s.solve(t(b16)).cpu().numpy()
+    s.status()
+    assert s.info()["cached_graphs"] == 0
+    x4.fill_(0.0)
+    with torch.cuda.stream(st):
+        s.graph_solve(b4d, x4, st)
+        s.graph_solve(b4d, x4, st)
+    st.synchronize()
+    s.status(st)
+    assert s.info()["cached_graphs"] == 1
+    x4h = x4.cpu().numpy()
+    so = m.sys_rowoff
+    for i in range(0, len(so) - 1, 9):
+        r0, r1 = so[i], so[i + 1]
+        k0, k1 = m.rowptr[r0], m.rowptr[r1]
+        rp, ci, v = m.rowptr[r0:r1 + 1] - k0, m.colidx[k0:k1] - r0, m.val[k0:k1]
+        assert rel_inf_err(x4h[r0:r1], oracle.solve_csr_lower(rp, ci, v, b4[r0:r1])) <= 1e-12
+        assert rel_inf_err(x16[r0:r1], oracle.solve_csr_lower(rp, ci, v, b16[r0:r1])) <= 1e-12
+    # settings that a capture bakes in drop the cache too
+    s.set_timeout(5.0)
+    assert s.info()["cached_graphs"] == 0
+
+
+def test_graph_solve_csc_first_call():
+    """A CSC handle's first solve through graph replay: the column visiting
+    order and the scratch are built before the capture starts."""
+    m = cs.generate("plain_20k", seed=0)
+    cp, ri, cv = cs.matrix_transposition(m.n, m.n, m.nnz, m.rowptr, m.colidx, m.val)
+    s = cs.TriangularSolver(t(cp), t(ri), t(cv), fmt="csc")
+    b = np.random.default_rng(3).standard_normal(m.n)
+    bd, x = t(b), torch.empty(m.n, dtype=torch.float64, device=DEV)
+    st = torch.cuda.Stream()
+    with torch.cuda.stream(st):
+        s.graph_solve(bd, x, st)
+        s.graph_solve(bd, x, st)
+    st.synchronize()
+    s.status(st)
+    assert rel_inf_err(x.cpu().numpy(), oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)) <= 1e-12
