@@ -4,19 +4,27 @@ Default workload (N=1): the plain FP64 solve of the 4,194,304-row wide-level
 matrix (1-7 off-diagonals per row in a band of 65,536; b = L*ones), the
 configuration the headline metric is quoted on.  One step = one complete
 solve (fill of x + the solve kernel) over inputs already resident in HBM.
+The same JSON line also carries the two forms, each measured against its
+per-system loop of plain solves (`forms`): the batched form (2,048 systems,
+k = 1 and 16 right-hand sides, one CUDA-graph replay per step) and the
+differentiation form (grad_1m, 16 RHS, forward + backward per step).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
                   [--workload wide_4m|plain_20k|zipf_1m|grad_1m|batched|autograd]
-                  [--dtype f64|f32]
+                  [--dtype f64|f32] [--no-forms]
 
 Output: one JSON line on rank 0.  `value` is GFLOP/s with (2*nnz - n) flops
 per solve (the benchmark definition's convention); `roofline` relates the
 solve kernel's algorithmic bytes (4(n+1) + 4nnz + 4n + s*nnz + 2*s*n, the
 reference's formula in CUDA/ourWrtFst/spts_syncfree_cuda_csr_wrt.h:208) per
-launch to its CUDA-event duration; `e2e` is the same metric through the
-host-buffer C-ABI call (capsp_solve_host: H2D of b, solve, D2H of x);
-`cpu_baseline` is the reference's serial executor on the host cores.
---impl reference times the reference's own CPU implementation instead.
+launch to its CUDA-event duration, and the kernel time to its dependency-chain
+floor (levels x the measured per-level hop); `e2e` is the same metric through
+the host-buffer C-ABI call (capsp_solve_host: b read from pinned host memory,
+x copied back); `cpu_baseline` is the reference's serial executor on the host
+cores.  --impl reference times the reference's own CPU implementation instead;
+that arm builds its inputs with the oracle library alone (the same seeded
+generator, compiled into oracle/_build/liboracle.so) and never loads the
+solver library.
 Multi-GPU: the solve is one dependency DAG and does not shard; --gpus N runs
 N independent replicas (one process per GPU) and reports the aggregate.
 """
@@ -55,6 +63,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-vendor", action="store_true", help="skip the cuSPARSE SpSV side-by-side")
     ap.add_argument("--nsys", type=int, default=0, help="systems in the batched workload (default 2,048)")
+    ap.add_argument("--no-forms", action="store_true", help="headline line without the batched/autograd forms")
+    ap.add_argument("--forms-cpu-seconds", type=float, default=5.0, help="CPU baseline sample of each form")
     return ap.parse_args()
 
 
@@ -168,43 +178,66 @@ def workload_matrix(name: str, dtype):
     return m, val, b
 
 
-def cpu_arm_runner(m, val):
+def cpu_arm_runner(rowptr, colidx, val):
     """The reference's serial executor (oracle/_ref when built here, else the oracle port)."""
     import oracle
     ref = oracle.ref()
     if ref is not None:
-        return ref.prepared_forward(m.rowptr, m.colidx, val), "reference"
-    return oracle.prepared_forward(m.rowptr, m.colidx, val), "port"
+        return ref.prepared_forward(rowptr, colidx, val), "reference"
+    return oracle.prepared_forward(rowptr, colidx, val), "port"
 
 
-def time_cpu(run, b, seconds: float, min_reps: int = 3):
+def serial_sample(run, b, solves: int, warmup: int):
+    """Per-solve wall times of `solves` full serial solves after `warmup` untimed
+    ones.  Both CPU legs (the reference arm and the native line's cpu_baseline)
+    use this, and both report the median."""
     x = np.empty_like(b)
+    for _ in range(warmup):
+        run(b, x)
     times = []
-    t_end = time.perf_counter() + seconds
-    while len(times) < min_reps or time.perf_counter() < t_end:
+    for _ in range(solves):
         t0 = time.perf_counter()
         run(b, x)
         times.append(time.perf_counter() - t0)
     return times, x
 
 
+def cpu_solves(args) -> int:
+    """Serial solves per CPU measurement: the timed steps, at least 20."""
+    return max(args.steps, 20)
+
+
 # ---------------------------------------------------------------------------
-# reference arm: the reference's CPU implementation of the path
+# reference arm: the reference's CPU implementation of the path, on inputs the
+# oracle library generates (the solver library is never loaded here)
 # ---------------------------------------------------------------------------
+
+def oracle_workload(name: str, dtype):
+    import oracle
+    n, rp, ci, v = oracle.generate(name, seed=0)
+    v = v.astype(dtype)
+    return n, rp, ci, v, oracle.get_x_b(rp, v)
+
+
+def oracle_batch_rhs(n, k):
+    import oracle
+    return oracle.normal(n * k, seed=0, stream=1000 + k).reshape(n, k)
+
 
 def run_reference_forms(args):
     """Reference serial executor on the batched / autograd workloads (bounded samples per step)."""
-    import capellinisptrsv_gb300 as cs
+    import oracle
+    W = oracle.workloads()
     if args.workload == "batched":
         k = args.nrhs or BATCH_KS[0]
-        m = cs.generate_batched(args.nsys or BATCH_NSYS, seed=0)
-        nsys = len(m.sys_rowoff) - 1
+        n, rp, ci, v, so = oracle.generate_batched(args.nsys or BATCH_NSYS, seed=0)
+        nsys = len(so) - 1
         picks = sorted(set(np.linspace(0, nsys - 1, 64).round().astype(int).tolist()))
-        rhs = _batch_rhs(cs, m.n, k)
+        rhs = oracle_batch_rhs(n, k)
         work = []
         for s in picks:
-            r0, r1, rp, ci, v = _sub_system(m, s)
-            run, kind = cpu_arm_runner(type(m)(r1 - r0, rp, ci, v), v)
+            r0, r1, srp, sci, sv = W.sub_system(rp, ci, v, so, s)
+            run, kind = cpu_arm_runner(srp, sci, sv)
             b = np.ascontiguousarray(rhs[r0:r1]) if k > 1 else rhs[r0:r1, 0].copy()
             work.append((run, b, np.empty_like(b)))
         # the systems are independent: one per host thread
@@ -222,17 +255,16 @@ def run_reference_forms(args):
     else:
         cores = 1  # one system: the executor takes all RHS in one serial call
         k = args.nrhs or AUTOGRAD_RHS
-        m = cs.generate("grad_1m", seed=0)
-        b_h = cs.normal(m.n * k, seed=0, stream=1).reshape(m.n, k)
-        xs_h = cs.normal(m.n * k, seed=0, stream=2).reshape(m.n, k)
-        import oracle
-        run, kind = cpu_arm_runner(m, m.val)
+        n, rp, ci, v = oracle.generate("grad_1m", seed=0)
+        b_h = oracle.normal(n * k, seed=0, stream=1).reshape(n, k)
+        xs_h = oracle.normal(n * k, seed=0, stream=2).reshape(n, k)
+        run, kind = cpu_arm_runner(rp, ci, v)
         adjoint = (oracle.ref() or oracle).solve_csr_transpose
 
         def one():
             x = run(b_h, np.empty_like(b_h))
-            y = adjoint(m.rowptr, m.colidx, m.val, x - xs_h)
-            oracle.grad_val(m.rowptr, m.colidx, y, x)
+            y = adjoint(rp, ci, v, x - xs_h)
+            oracle.grad_val(rp, ci, y, x)
         per_step, unit = None, "ms"
         metric = f"fwd+bwd ms ({k} RHS)"
         sample = f"full grad_1m fwd+bwd with {k} RHS per step (steps capped at 10)"
@@ -245,7 +277,7 @@ def run_reference_forms(args):
         t0 = time.perf_counter()
         one()
         t.append(time.perf_counter() - t0)
-    sec = statistics.mean(t)
+    sec = statistics.median(t)
     value = per_step / sec if per_step else sec * 1e3
     line = {
         "impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": args.gpus, "gpus_used": 0,
@@ -253,9 +285,9 @@ def run_reference_forms(args):
         "warmup": min(args.warmup, 3), "ms_per_step": sec * 1e3, "higher_is_better": hib, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, seed 0)",
         "config": {"workload": args.workload, "rhs": k},
-        "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": kind, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "host_cores": os.cpu_count(), "kind": kind,
+                         "sample": sample + " (median step)"},
         "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "host_cores_available": os.cpu_count(),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -268,31 +300,27 @@ def run_reference(args):
     if args.workload in ("batched", "autograd"):
         return run_reference_forms(args)
     dt = np.float64 if args.dtype == "f64" else np.float32
-    m, val, b = workload_matrix(args.workload, dt)
-    run, kind = cpu_arm_runner(m, val)
-    x = np.empty_like(b)
-    for _ in range(args.warmup):
-        run(b, x)
-    steps = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        run(b, x)
-        steps.append(time.perf_counter() - t0)
-    flops = 2.0 * m.nnz - m.n
-    sec = sum(steps) / len(steps)
+    n, rp, ci, val, b = oracle_workload(args.workload, dt)
+    nnz = int(rp[-1])
+    run, kind = cpu_arm_runner(rp, ci, val)
+    steps, _ = serial_sample(run, b, args.steps, args.warmup)
+    flops = 2.0 * nnz - n
+    sec = statistics.median(steps)
     val_gf = flops / sec / 1e9
     line = {
         "impl": "reference", "metric": "SpTRSV GFLOP/s (2*nnz-n flops per solve)", "value": val_gf,
         "unit": "GFLOP/s", "n_gpus": args.gpus, "gpus_used": 0, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": args.dtype, "data": "synthetic (seeded generator, seed 0)",
-        "config": {"workload": args.workload, "n": m.n, "nnz": m.nnz, "rhs": 1,
+        "config": {"workload": args.workload, "n": n, "nnz": nnz, "rhs": 1,
                    "l2": "host run; inputs larger than the last-level cache"},
-        "cpu_baseline": {"value": val_gf, "unit": "GFLOP/s", "cores": 1, "kind": kind,
-                         "sample": f"{args.steps} full serial solves of the {args.workload} matrix "
-                                   "(sptrsv_syncfree_executor FORWARD; transpose and in-degree analysis excluded)"},
+        "cpu_baseline": {"value": val_gf, "unit": "GFLOP/s", "cores": 1, "host_cores": os.cpu_count(), "kind": kind,
+                         "sample": f"{args.steps} full serial solves of the {args.workload} matrix after "
+                                   f"{args.warmup} untimed (median; sptrsv_syncfree_executor FORWARD; transpose "
+                                   "and in-degree analysis excluded)",
+                         "mean_ms": statistics.mean(steps) * 1e3},
         "e2e": {"value": val_gf, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "gflops_2nnz": 2.0 * m.nnz / sec / 1e9, "host_cores_available": os.cpu_count(),
+        "gflops_2nnz": 2.0 * nnz / sec / 1e9,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -303,18 +331,31 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 
 def run_native(args):
+    world, rank, local = dist_env()
+    dt = np.float64 if args.dtype == "f64" else np.float32
+    s_bytes = 8 if dt == np.float64 else 4
+    m, val, b = workload_matrix(args.workload, dt)
+    flops = 2.0 * m.nnz - m.n
+    # CPU baseline first, before this process initialises CUDA, with the same
+    # procedure and estimator as the reference arm (median of the same solves)
+    cpu, xc = None, None
+    if rank == 0 and not args.no_cpu_baseline:
+        run, kind = cpu_arm_runner(m.rowptr, m.colidx, val)
+        times, xc = serial_sample(run, b, cpu_solves(args), args.warmup)
+        tmed = statistics.median(times)
+        cpu = {"value": flops / tmed / 1e9, "unit": "GFLOP/s", "cores": 1, "host_cores": os.cpu_count(),
+               "kind": kind, "mean_ms": statistics.mean(times) * 1e3,
+               "sample": f"{len(times)} full serial solves of the {args.workload} matrix after {args.warmup} untimed "
+                         f"({sum(times):.1f} s; median; sptrsv_syncfree_executor FORWARD, transpose excluded)"}
+
     import torch
     import capellinisptrsv_gb300 as cs
-    world, rank, local = dist_env()
     if world > 1:
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     dev = torch.device("cuda", local if world > 1 else 0)
     torch.cuda.set_device(dev)
-    dt = np.float64 if args.dtype == "f64" else np.float32
-    s_bytes = 8 if dt == np.float64 else 4
-    m, val, b = workload_matrix(args.workload, dt)
     to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
     rp_d, ci_d, val_d, b_d = to(m.rowptr), to(m.colidx), to(val), to(b)
     solver = cs.TriangularSolver(rp_d, ci_d, val_d)
@@ -355,12 +396,16 @@ def run_native(args):
     xh = x_d.cpu().numpy()
     max_dev = float(np.max(np.abs(xh - 1.0)))
 
-    flops = 2.0 * m.nnz - m.n
     value = replica_value(world, flops, ms)
     alg_bytes = algorithmic_bytes(m.n, m.nnz, s_bytes)
     peak, peak_kind = peaks()
     achieved = alg_bytes / (kms * 1e-3) / 1e9
     traffic = profile_traffic("row_solve", args.workload + "_" + args.dtype)
+    info = solver.info()
+    # dependency-chain floor: a solve of L levels takes at least L - 1 hops,
+    # each costing at least one publication's detection on another warp
+    hop_ns = cs.hop_latency(n=262_144, stride=64, dtype=dt)
+    floor_ms = max(info["levels"] - 1, 0) * hop_ns * 1e-6
 
     line = None
     if rank == 0:
@@ -368,24 +413,13 @@ def run_native(args):
         if not args.no_e2e:
             e2e = e2e_measure(cs, m, val, b, args, flops)
         vendor = None if args.no_vendor else vendor_measure(m, rp_d, ci_d, val_d, b_d, args, flops, kms)
-        cpu = None
-        if not args.no_cpu_baseline:
-            run, kind = cpu_arm_runner(m, val)
-            times, xc = time_cpu(run, b, args.cpu_seconds)
-            tmed = statistics.median(times)
-            cpu = {"value": flops / tmed / 1e9, "unit": "GFLOP/s", "cores": 1, "kind": kind,
-                   "sample": f"{len(times)} full serial solves of the {args.workload} matrix in {sum(times):.1f} s "
-                             "(median; sptrsv_syncfree_executor FORWARD, transpose excluded)"}
-            rel = float(np.max(np.abs(xh - xc)) / np.max(np.abs(xc)))
-        else:
-            rel = None
-        info = solver.info()
+        rel = float(np.max(np.abs(xh - xc)) / np.max(np.abs(xc))) if xc is not None else None
         line = {
             "metric": "SpTRSV GFLOP/s (2*nnz-n flops per solve)", "value": value, "unit": "GFLOP/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
             "data": "synthetic (seeded generator, seed 0; stands in for the SuiteSparse set)",
-            "config": {"workload": args.workload, "n": m.n, "nnz": m.nnz, "rhs": 1,
+            "config": {"workload": args.workload, "n": m.n, "nnz": m.nnz, "rhs": 1, "levels": info["levels"],
                        "algorithm": {1: "wrtfst", 2: "twopart", 3: "mix"}.get(info["algorithm"], "auto"),
                        "rows_per_thread": info["rows_per_thread"], "block": info["block_threads"],
                        "l2": "flushed between steps (512 MiB write outside the timed events); "
@@ -394,7 +428,12 @@ def run_native(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "row_solve_kernel", "kernel_ms": kms,
-                         "algorithmic_bytes_per_launch": alg_bytes},
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "hop_ns": hop_ns, "latency_floor_ms": floor_ms,
+                         "frac_of_floor": floor_ms / kms if kms > 0 else None,
+                         "floor_how": "(levels - 1) x the per-level time of a chain matrix whose levels are "
+                                      "64 rows in two warps, each row waiting on one row of the level before "
+                                      "(capsp_hop_latency, n=262,144, stride 64, same dtype), measured live"},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "cusparse_spsv": vendor,
@@ -405,6 +444,12 @@ def run_native(args):
             "wall_s_timed_region": t_wall,
             "clocks": clk.summary(),
         }
+    solver.close()
+    del rp_d, ci_d, val_d, b_d, x_d, flush
+    if rank == 0 and world == 1 and not args.no_forms and args.workload == "wide_4m":
+        torch.cuda.empty_cache()
+        line["forms"] = measure_forms(args)
+    if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -497,10 +542,8 @@ AUTOGRAD_RHS = 16
 
 def _sub_system(m, s):
     """Rows [r0, r1) of system s as a standalone CSR (indices rebased)."""
-    r0, r1 = int(m.sys_rowoff[s]), int(m.sys_rowoff[s + 1])
-    k0, k1 = int(m.rowptr[r0]), int(m.rowptr[r1])
-    return (r0, r1, np.ascontiguousarray(m.rowptr[r0:r1 + 1] - k0, dtype=np.int32),
-            np.ascontiguousarray(m.colidx[k0:k1] - r0, dtype=np.int32), np.ascontiguousarray(m.val[k0:k1]))
+    from capellinisptrsv_gb300 import workloads as W
+    return W.sub_system(m.rowptr, m.colidx, m.val, m.sys_rowoff, s)
 
 
 def _single_gpu_forms(args):
@@ -529,46 +572,58 @@ def _run_all(pool, work):
 
 def _cpu_batched(cs, m, k, seconds):
     """Reference serial executor, one system per host thread (the systems are
-    independent; each group is prepared outside the clock)."""
+    independent; each group is prepared outside the clock).  Returns the rate
+    and the solutions of the systems it solved, (r0, r1, x) each."""
     from concurrent.futures import ThreadPoolExecutor
     threads = host_threads()
     rhs = _batch_rhs(cs, m.n, k)
     nsys = len(m.sys_rowoff) - 1
     run_kind = None
     solved, spent, systems, s = 0, 0.0, 0, 0
+    sols = []
     with ThreadPoolExecutor(threads) as pool:
         while s < nsys and spent < seconds:
-            work = []
+            work, rows = [], []
             for _ in range(4 * threads):
                 if s >= nsys:
                     break
                 r0, r1, rp, ci, v = _sub_system(m, s)
-                run, run_kind = cpu_arm_runner(type(m)(r1 - r0, rp, ci, v), v)
+                run, run_kind = cpu_arm_runner(rp, ci, v)
                 b = np.ascontiguousarray(rhs[r0:r1]) if k > 1 else rhs[r0:r1, 0].copy()
                 work.append((run, b, np.empty_like(b)))
+                rows.append((r0, r1))
                 s += 1
             t0 = time.perf_counter()
             _run_all(pool, work)
             spent += time.perf_counter() - t0
             solved += len(work) * k
             systems += len(work)
-    return solved / spent, run_kind, systems, spent, threads
+            sols.extend((r0, r1, w[2]) for (r0, r1), w in zip(rows, work))
+    return solved / spent, run_kind, systems, spent, threads, sols
 
 
-def run_batched(args):
+def _rel(a, r) -> float:
+    a, r = np.asarray(a, np.float64), np.asarray(r, np.float64)
+    return float(np.max(np.abs(a - r)) / max(np.max(np.abs(r)), 1e-300))
+
+
+def measure_batched(args, ks, cpu_seconds, e2e: bool = True):
+    """The batched form on one GPU: per k, one CUDA-graph replay per step
+    against a loop of single-RHS plain solves; the CPU baseline (and the
+    result check against it) and e2e at the first k."""
     import ctypes as C
     import torch
     import capellinisptrsv_gb300 as cs
     from capellinisptrsv_gb300 import _native as N
-    _single_gpu_forms(args)
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     m = cs.generate_batched(args.nsys or BATCH_NSYS, seed=0)
     nsys = len(m.sys_rowoff) - 1
     to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
     rp_d, ci_d, val_d = to(m.rowptr), to(m.colidx), to(m.val)
+    t0 = time.perf_counter()
     batch = cs.TriangularSolver(rp_d, ci_d, val_d, sys_rowoff=m.sys_rowoff)
-    ks = [args.nrhs] if args.nrhs else list(BATCH_KS)
+    analyse_s = time.perf_counter() - t0
     st = torch.cuda.Stream(dev)
     sth = C.c_void_p(st.cuda_stream)
 
@@ -583,6 +638,7 @@ def run_batched(args):
 
     peak, peak_kind = peaks()
     sweep = []
+    x_first = None
     for k in ks:
         b_h = _batch_rhs(cs, m.n, k)
         b_d = to(b_h if k > 1 else b_h[:, 0])
@@ -641,14 +697,14 @@ def run_batched(args):
         loop_ms = e0.elapsed_time(e1) / loop_steps
         # the loop's results against the batched launch's
         xb = x_d.cpu().numpy().reshape(m.n, -1)
+        if x_first is None:
+            x_first = xb
         worst, c = 0.0, 0
         for s in picks:
             r0, r1, _ = handles[s]
             for j in range(k):
-                xl = cols[c][2].cpu().numpy()
+                worst = max(worst, _rel(cols[c][2].cpu().numpy(), xb[r0:r1, j]))
                 c += 1
-                ref = xb[r0:r1, j]
-                worst = max(worst, float(np.max(np.abs(xl - ref)) / max(np.max(np.abs(ref)), 1e-300)))
         solves = nsys * k
         entry = {
             "k": k, "solves_per_s": solves / (ms * 1e-3), "ms_per_step": ms, "kernel_ms": kms,
@@ -660,51 +716,74 @@ def run_batched(args):
         }
         entry["speedup_vs_loop"] = entry["solves_per_s"] / entry["loop_solves_per_s"]
         alg = algorithmic_bytes(m.n, m.nnz, 8, k)
-        # DRAM bytes per launch from the committed capture (single RHS, default batch)
-        traffic = profile_traffic("row_solve", "batched_f64") if k == 1 and nsys == BATCH_NSYS else None
+        # DRAM bytes per launch from a committed capture of this k (default batch)
+        traffic = profile_traffic("row_solve", f"batched_k{k}_f64") if nsys == BATCH_NSYS else None
         entry["roofline"] = {"bound": "hbm", "achieved": alg / (kms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                              "frac": alg / (kms * 1e-3) / 1e9 / peak, "traffic": traffic, "peak_kind": peak_kind,
                              "kernel": "row_solve_kernel", "kernel_ms": kms, "algorithmic_bytes_per_launch": alg}
         sweep.append(entry)
         del b_d, x_d, cols, calls
 
-    head = sweep[0]
-    k = head["k"]
-    # end to end through the host-buffer call: pinned b in, x out, every step
-    b_h = _batch_rhs(cs, m.n, k)
-    b_h = b_h if k > 1 else b_h[:, 0].copy()
-    bh = torch.from_numpy(np.ascontiguousarray(b_h)).pin_memory()
-    xh = torch.empty_like(bh).pin_memory()
-    batch.solve_host(bh.numpy(), xh.numpy())
-    reps = max(3, min(args.steps, 20))
-    t0 = time.perf_counter()
-    for _ in range(reps):
+    k = ks[0]
+    out = {"nsys": nsys, "n": m.n, "nnz": m.nnz, "levels": batch.info()["levels"], "analyse_s": analyse_s,
+           "sweep": sweep}
+    if e2e:
+        # end to end through the host-buffer call: pinned b in, x out, every step
+        b_h = _batch_rhs(cs, m.n, k)
+        b_h = b_h if k > 1 else b_h[:, 0].copy()
+        bh = torch.from_numpy(np.ascontiguousarray(b_h)).pin_memory()
+        xh = torch.empty_like(bh).pin_memory()
         batch.solve_host(bh.numpy(), xh.numpy())
-    e2e_s = (time.perf_counter() - t0) / reps
-    cpu = None
-    if not args.no_cpu_baseline:
-        v, kind, systems, spent, threads = _cpu_batched(cs, m, k, args.cpu_seconds)
-        cpu = {"value": v, "unit": "solves/s", "cores": threads, "kind": kind,
-               "sample": f"first {systems} of {nsys} systems x {k} RHS in {spent:.1f} s, one system per host "
-                         f"thread on {threads} threads (sptrsv_syncfree_executor FORWARD; transpose and "
-                         "analysis excluded)"}
+        reps = max(3, min(args.steps, 20))
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            batch.solve_host(bh.numpy(), xh.numpy())
+        e2e_s = (time.perf_counter() - t0) / reps
+        out["e2e"] = {"value": nsys * k / e2e_s, "unit": "solves/s", "rhs": k,
+                      "h2d_bytes_per_step": int(bh.numel() * 8), "d2h_bytes_per_step": int(xh.numel() * 8),
+                      "ms_per_step": e2e_s * 1e3}
+    out["cpu_baseline"] = None
+    if cpu_seconds > 0:
+        v, kind, systems, spent, threads, sols = _cpu_batched(cs, m, k, cpu_seconds)
+        out["cpu_baseline"] = {
+            "value": v, "unit": "solves/s", "rhs": k, "cores": threads, "host_cores": os.cpu_count(), "kind": kind,
+            "sample": f"first {systems} of {nsys} systems x {k} RHS in {spent:.1f} s, one system per host "
+                      f"thread on {threads} threads (sptrsv_syncfree_executor FORWARD; transpose and "
+                      "analysis excluded)"}
+        # the batched GPU result against the serial executor's, system by system
+        out["rel_err_vs_cpu_reference"] = max(_rel(x_first[r0:r1].reshape(r1 - r0, -1), xs.reshape(r1 - r0, -1))
+                                             for r0, r1, xs in sols)
+        out["systems_checked_vs_cpu_reference"] = len(sols)
+    batch.close()
+    for _, _, hs in handles.values():
+        hs.close()
+    return out
+
+
+def run_batched(args):
+    _single_gpu_forms(args)
+    ks = [args.nrhs] if args.nrhs else list(BATCH_KS)
+    d = measure_batched(args, ks, 0.0 if args.no_cpu_baseline else args.cpu_seconds)
+    head = d["sweep"][0]
+    k = head["k"]
     line = {
-        "metric": f"batched solves/s ({nsys} systems x k RHS)", "value": head["solves_per_s"], "unit": "solves/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": head["ms_per_step"],
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded generator, seed 0)",
-        "config": {"workload": "batched", "nsys": nsys, "n": m.n, "nnz": m.nnz, "rhs": k,
+        "metric": f"batched solves/s ({d['nsys']} systems x k RHS)", "value": head["solves_per_s"],
+        "unit": "solves/s", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup),
+        "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded generator, seed 0)",
+        "config": {"workload": "batched", "nsys": d["nsys"], "n": d["n"], "nnz": d["nnz"], "rhs": k,
+                   "levels": d["levels"],
                    "launch": "CUDA graph replay of one persistent solve (autotuned launch shape)",
-                   "l2": f"inputs ({algorithmic_bytes(m.n, m.nnz, 8, k) / 1e9:.1f} GB) larger than L2, no flush",
+                   "l2": f"inputs ({algorithmic_bytes(d['n'], d['nnz'], 8, k) / 1e9:.1f} GB) larger than L2, "
+                         "no flush",
                    "parallelism": "single GPU"},
-        "roofline": head["roofline"], "cpu_baseline": cpu,
-        "e2e": {"value": nsys * k / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(bh.numel() * 8),
-                "d2h_bytes_per_step": int(xh.numel() * 8), "ms_per_step": e2e_s * 1e3},
+        "roofline": head["roofline"], "cpu_baseline": d["cpu_baseline"], "e2e": d["e2e"],
         "gpu_launches": 2 * args.steps,
         "loop_baseline": {"value": head["loop_solves_per_s"], "unit": "solves/s",
                           "what": "one single-RHS capsp_solve per system and RHS column, each system on its own "
                                   "handle, on an evenly spaced sample of systems"},
-        "speedup_vs_loop": head["speedup_vs_loop"], "sweep": sweep, "clocks": head["clocks"],
+        "speedup_vs_loop": head["speedup_vs_loop"], "sweep": d["sweep"], "clocks": head["clocks"],
+        "rel_err_vs_cpu_reference": d.get("rel_err_vs_cpu_reference"),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -715,13 +794,14 @@ def _transpose_bytes(n, nnz, s, k):
     return 4.0 * (n + 1) + 4.0 * nnz + s * nnz + 4.0 * n + 3.0 * s * n * k + s * nnz
 
 
-def run_autograd(args):
+def measure_autograd(args, cpu_seconds):
+    """The differentiation form: forward + backward through SparseTriangularSolve
+    against a loop of single-RHS solves; CPU fwd+bwd and the result check against it."""
     import torch
     import capellinisptrsv_gb300 as cs
-    _single_gpu_forms(args)
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    k = args.nrhs or AUTOGRAD_RHS
+    k = args.nrhs if (args.nrhs and args.workload == "autograd") else AUTOGRAD_RHS
     m = cs.generate("grad_1m", seed=0)
     n = m.n
     to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
@@ -763,6 +843,7 @@ def run_autograd(args):
     solver.solve_transpose_grad((x - xstar).contiguous(), x)
     kb = solver.last_kernel_ms()
     solver.set_profiling(False)
+    x_gpu = x.cpu().numpy()
 
     # loop arm: single-RHS solves of L and of an explicitly transposed L
     cp, ri, cv = cs.matrix_transposition(n, n, m.nnz, m.rowptr, m.colidx, m.val)
@@ -815,57 +896,110 @@ def run_autograd(args):
     peak, peak_kind = peaks()
     fwd_bytes = algorithmic_bytes(n, m.nnz, 8, k)
     bwd_bytes = _transpose_bytes(n, m.nnz, 8, k)
-    if kb >= kf:
-        roof = {"kernel": "col_solve_kernel (transpose solve + grad_val)", "kernel_ms": kb,
-                "algorithmic_bytes_per_launch": bwd_bytes, "achieved": bwd_bytes / (kb * 1e-3) / 1e9}
-    else:
-        roof = {"kernel": "row_solve_kernel (forward)", "kernel_ms": kf,
-                "algorithmic_bytes_per_launch": fwd_bytes, "achieved": fwd_bytes / (kf * 1e-3) / 1e9}
-    # DRAM bytes of the captured column launch (grad_1m, 16 RHS) when that is the one reported
-    traffic = profile_traffic("col_solve", f"grad_1m_{k}rhs_f64") if kb >= kf else None
-    roof.update({"bound": "hbm", "peak": peak, "unit": "GB/s", "frac": roof["achieved"] / peak,
-                 "traffic": traffic, "peak_kind": peak_kind})
-    cpu = None
-    if not args.no_cpu_baseline:
-        cpu = _cpu_autograd(m, b_h, xs_h, args.cpu_seconds)
+    kernels = {
+        "forward_row_solve": {"kernel": "row_solve_kernel", "kernel_ms": kf, "algorithmic_bytes_per_launch": fwd_bytes,
+                              "achieved": fwd_bytes / (kf * 1e-3) / 1e9,
+                              "traffic": profile_traffic("row_solve", f"grad_1m_{k}rhs_f64")},
+        "transpose_solve_grad": {"kernel": "col_solve_packed_kernel (transpose solve + fused grad_val)",
+                                 "kernel_ms": kb, "algorithmic_bytes_per_launch": bwd_bytes,
+                                 "achieved": bwd_bytes / (kb * 1e-3) / 1e9,
+                                 "traffic": profile_traffic("col_solve", f"grad_1m_{k}rhs_f64")},
+    }
+    for r in kernels.values():
+        r.update({"bound": "hbm", "peak": peak, "unit": "GB/s", "frac": r["achieved"] / peak, "peak_kind": peak_kind})
+    roof = kernels["transpose_solve_grad"] if kb >= kf else kernels["forward_row_solve"]
+    out = {"n": n, "nnz": m.nnz, "rhs": k, "ms_per_step": ms, "kernel_ms": {"forward_row_solve": kf,
+                                                                              "transpose_solve_grad": kb},
+           "roofline": roof, "kernels": kernels,
+           "loop_baseline": {"value": loop_ms, "unit": "ms",
+                             "what": f"{k} single-RHS solves of L + {k} single-RHS solves of an explicit L^T "
+                                     "(upper CSR) + one grad_val pass"},
+           "speedup_vs_loop": loop_ms / ms, "loop_vs_autograd_rel_err": agree, "clocks": clk.summary(),
+           "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(2 * n * k * 8), "d2h_bytes_per_step": 8},
+           # forward: 1/diag + level-value refresh, pending fill, row solve;
+           # backward: 1/diag + level-value refresh, column solve (fused grad_val)
+           "gpu_launches_per_step": 7}
+    out["cpu_baseline"] = None
+    if cpu_seconds > 0:
+        cpu, (xc, yc, gc) = _cpu_autograd(m, b_h, xs_h, cpu_seconds)
+        out["cpu_baseline"] = cpu
+        # the GPU gradients against the serial forward / adjoint / grad_val
+        out["rel_err_vs_cpu_reference"] = {"x": _rel(x_gpu, xc), "grad_b": _rel(g_b.cpu().numpy(), yc),
+                                           "grad_val": _rel(g_val.cpu().numpy(), gc)}
+    solver.close()
+    upper.close()
+    return out
+
+
+def run_autograd(args):
+    _single_gpu_forms(args)
+    d = measure_autograd(args, 0.0 if args.no_cpu_baseline else args.cpu_seconds)
+    k = d["rhs"]
     line = {
-        "metric": f"fwd+bwd ms ({k} RHS)", "value": ms, "unit": "ms", "n_gpus": 1, "steps": args.steps,
-        "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, seed 0)",
-        "config": {"workload": "autograd", "matrix": "grad_1m", "n": n, "nnz": m.nnz, "rhs": k,
+        "metric": f"fwd+bwd ms ({k} RHS)", "value": d["ms_per_step"], "unit": "ms", "n_gpus": 1, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": d["ms_per_step"], "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, seed 0)",
+        "config": {"workload": "autograd", "matrix": "grad_1m", "n": d["n"], "nnz": d["nnz"], "rhs": k,
                    "loss": "0.5*||x - x*||^2",
                    "l2": "inputs (matrix, b, x, x*) larger than L2, no flush", "parallelism": "single GPU"},
-        "roofline": roof, "cpu_baseline": cpu,
-        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(2 * n * k * 8), "d2h_bytes_per_step": 8},
-        # forward: 1/diag + level-value refresh, pending fill, row solve;
-        # backward: 1/diag + level-value refresh, column solve (fused grad_val)
-        "gpu_launches": 7 * args.steps,
-        "kernel_ms": {"forward_row_solve": kf, "transpose_solve_grad": kb},
-        "loop_baseline": {"value": loop_ms, "unit": "ms",
-                          "what": f"{k} single-RHS solves of L + {k} single-RHS solves of an explicit L^T "
-                                  "(upper CSR) + one grad_val pass"},
-        "speedup_vs_loop": loop_ms / ms, "loop_vs_autograd_rel_err": agree, "clocks": clk.summary(),
+        "roofline": d["roofline"], "cpu_baseline": d["cpu_baseline"], "e2e": d["e2e"],
+        "gpu_launches": d["gpu_launches_per_step"] * args.steps,
+        "kernel_ms": d["kernel_ms"], "kernels": d["kernels"], "loop_baseline": d["loop_baseline"],
+        "speedup_vs_loop": d["speedup_vs_loop"], "loop_vs_autograd_rel_err": d["loop_vs_autograd_rel_err"],
+        "rel_err_vs_cpu_reference": d.get("rel_err_vs_cpu_reference"), "clocks": d["clocks"],
     }
     print(json.dumps(line), flush=True)
     return 0
 
 
 def _cpu_autograd(m, b_h, xs_h, seconds):
-    """Serial forward (k RHS), serial adjoint (BACKWARD executor on L's CSR) and grad_val."""
+    """Serial forward (k RHS), serial adjoint (BACKWARD executor on L's CSR) and
+    grad_val, median over passes; also returns the last pass's (x, y, grad_val)."""
     import oracle
-    run, kind = cpu_arm_runner(m, m.val)
+    run, kind = cpu_arm_runner(m.rowptr, m.colidx, m.val)
     adjoint = (oracle.ref() or oracle).solve_csr_transpose
     times = []
     t_end = time.perf_counter() + seconds
+    res = None
     while not times or time.perf_counter() < t_end:
         t0 = time.perf_counter()
         x = run(b_h, np.empty_like(b_h))
         y = adjoint(m.rowptr, m.colidx, m.val, x - xs_h)
-        oracle.grad_val(m.rowptr, m.colidx, y, x)
+        g = oracle.grad_val(m.rowptr, m.colidx, y, x)
         times.append(time.perf_counter() - t0)
-    return {"value": statistics.median(times) * 1e3, "unit": "ms", "cores": 1, "kind": kind,
-            "sample": f"{len(times)} serial fwd+bwd passes over the full grad_1m system with "
-                      f"{b_h.shape[1]} RHS (median)"}
+        res = (x, y, g)
+    return {"value": statistics.median(times) * 1e3, "unit": "ms", "cores": 1, "host_cores": os.cpu_count(),
+            "kind": kind, "sample": f"{len(times)} serial fwd+bwd passes over the full grad_1m system with "
+                                    f"{b_h.shape[1]} RHS (median)"}, res
+
+
+FORMS_KS = (1, 16)
+
+
+def measure_forms(args):
+    """Both forms at their benchmark sizes, compacted for the headline line."""
+    bt = measure_batched(args, FORMS_KS, args.forms_cpu_seconds, e2e=True)
+    batched = {
+        "metric": "solves/s", "nsys": bt["nsys"], "n": bt["n"], "nnz": bt["nnz"], "levels": bt["levels"],
+        "launch": "CUDA graph replay of one persistent solve (autotuned launch shape)",
+        "per_k": {str(e["k"]): {key: e[key] for key in ("solves_per_s", "ms_per_step", "kernel_ms",
+                                                         "loop_solves_per_s", "speedup_vs_loop", "roofline",
+                                                         "loop_vs_batched_rel_err", "clocks")}
+                  for e in bt["sweep"]},
+        "loop_what": "one single-RHS capsp_solve per system and RHS column, each system on its own handle, "
+                     "on an evenly spaced sample of systems",
+        "cpu_baseline": bt["cpu_baseline"], "e2e": bt.get("e2e"),
+        "rel_err_vs_cpu_reference": bt.get("rel_err_vs_cpu_reference"),
+        "systems_checked_vs_cpu_reference": bt.get("systems_checked_vs_cpu_reference"),
+    }
+    ag = measure_autograd(args, args.forms_cpu_seconds)
+    autograd = {key: ag[key] for key in ("n", "nnz", "rhs", "ms_per_step", "kernel_ms", "kernels", "loop_baseline",
+                                          "speedup_vs_loop", "loop_vs_autograd_rel_err", "cpu_baseline", "e2e",
+                                          "clocks")}
+    autograd["metric"] = "fwd+bwd ms"
+    autograd["rel_err_vs_cpu_reference"] = ag.get("rel_err_vs_cpu_reference")
+    return {"batched": batched, "autograd": autograd,
+            "steps": args.steps, "warmup": max(3, args.warmup), "dtype": "f64"}
 
 
 def main():

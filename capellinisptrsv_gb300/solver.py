@@ -21,6 +21,7 @@ from typing import Optional
 import numpy as np
 
 from . import _native as N
+from . import workloads as W
 
 try:  # torch is plumbing for device memory and streams
     import torch
@@ -76,23 +77,9 @@ class CSRMatrix:
         return digest(self.n, self.rowptr, self.colidx, self.val)
 
 
-# The five seeded workloads of the benchmark definition.  Shared value rule:
-# off-diagonals U[-1,1], diagonal 1 + sum|off-diagonals| (last in its row).
-WORKLOADS = {
-    # n=20,000; k~U{1..5} distinct columns in [max(0,i-2000), i-1]; b = L*ones
-    "plain_20k": dict(n=20_000, kind=N.GEN_UNIFORM_BAND, kmin=1, kmax=5, band=2000),
-    # n=4,194,304; k~U{1..7} (mean 4) in [max(0,i-65536), i-1]; b = L*ones
-    "wide_4m": dict(n=4_194_304, kind=N.GEN_UNIFORM_BAND, kmin=1, kmax=7, band=65536),
-    # n=1,048,576; k~Zipf(1.8) on 1..512; ceil(k/2) cols in [i-32, i-1], the rest in [0, i-1]
-    # (a literal Zipf(1.8): 6.96 off-diagonals per row on average, ~126k levels)
-    "zipf_1m": dict(n=1_048_576, kind=N.GEN_ZIPF_NEAR_FAR, zipf_s=1.8, zipf_cap=512, near_window=32),
-    # the same with the count floored at 38, which brings the mean to ~40 off-diagonals
-    # per row; 19 of the previous 32 rows per row make it a near-serial chain
-    "zipf40_1m": dict(n=1_048_576, kind=N.GEN_ZIPF_NEAR_FAR, kmin=38, zipf_s=1.8, zipf_cap=512,
-                      near_window=32),
-    # n=1,048,576; k~U{2..10} (mean 6) in a band of 16,384 (differentiation workload)
-    "grad_1m": dict(n=1_048_576, kind=N.GEN_UNIFORM_BAND, kmin=2, kmax=10, band=16384),
-}
+# The seeded workloads of the benchmark definition (generator parameters in
+# workloads.py, shared with the oracle's copy of the generator).
+WORKLOADS = W.WORKLOADS
 
 
 def _gen_params(n, seed=0, stream=0, kind=N.GEN_UNIFORM_BAND, kmin=1, kmax=5, band=0,
@@ -108,10 +95,9 @@ def generate(workload: str | None = None, *, seed: int = 0, stream: int = 0, **p
     without a workload, describe the matrix (n, kind, kmin, kmax, band, zipf_s,
     zipf_cap, near_window).
     """
-    spec = dict(WORKLOADS[workload]) if workload else {}
-    spec.update(params)
-    p = _gen_params(seed=seed, stream=stream, **spec)
-    n = int(spec["n"])
+    sp = W.spec(workload, **params)
+    p = _gen_params(seed=seed, stream=stream, **sp)
+    n = int(sp["n"])
     rowptr = np.empty(n + 1, dtype=np.int32)
     N.check(N.lib.capsp_gen_rowptr(C.byref(p), _ptr(rowptr)))
     nnz = int(rowptr[-1])
@@ -130,28 +116,13 @@ def generate_batched(nsys: int = 2048, *, seed: int = 0, nmin: int = 500, nmax: 
     band of n_s // band_div; its rows come from generator stream s + 1.
     Column indices are global; ``sys_rowoff`` holds the first row of each system.
     """
-    rng = np.random.default_rng(seed)
-    sizes = np.rint(np.exp(rng.uniform(np.log(nmin), np.log(nmax), size=nsys))).astype(np.int64)
-    rowoff = np.zeros(nsys + 1, dtype=np.int64)
-    np.cumsum(sizes, out=rowoff[1:])
-    parts = [generate(n=int(sizes[s]), kind=N.GEN_UNIFORM_BAND, kmin=kmin, kmax=kmax,
-                      band=max(1, int(sizes[s]) // band_div), seed=seed, stream=s + 1)
-             for s in range(nsys)]
-    nnz_off = np.zeros(nsys + 1, dtype=np.int64)
-    np.cumsum([p.nnz for p in parts], out=nnz_off[1:])
-    if nnz_off[-1] >= 2**31 or rowoff[-1] >= 2**31:
-        raise ValueError("batch exceeds 32-bit indices")
-    n = int(rowoff[-1])
-    rowptr = np.empty(n + 1, dtype=np.int32)
-    colidx = np.empty(int(nnz_off[-1]), dtype=np.int32)
-    val = np.empty(int(nnz_off[-1]), dtype=np.float64)
-    for s, p in enumerate(parts):
-        r0, r1, k0 = int(rowoff[s]), int(rowoff[s + 1]), int(nnz_off[s])
-        rowptr[r0:r1] = p.rowptr[:-1] + k0
-        colidx[k0:k0 + p.nnz] = p.colidx + r0
-        val[k0:k0 + p.nnz] = p.val
-    rowptr[n] = int(nnz_off[-1])
-    return CSRMatrix(n, rowptr, colidx, val, rowoff.astype(np.int32))
+    sizes = W.batched_sizes(nsys, seed, nmin, nmax)
+    parts = []
+    for s in range(nsys):
+        m = generate(seed=seed, stream=s + 1, **W.batched_system_spec(sizes[s], kmin, kmax, band_div))
+        parts.append((m.rowptr, m.colidx, m.val))
+    n, rowptr, colidx, val, rowoff = W.assemble_batched(parts, sizes)
+    return CSRMatrix(n, rowptr, colidx, val, rowoff)
 
 
 def normal(count: int, *, seed: int = 0, stream: int = 0) -> np.ndarray:

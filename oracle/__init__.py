@@ -3,12 +3,18 @@
 ctypes access to (1) liboracle.so, the C restatement of the reference's serial
 sync-free solve (oracle.c), and (2) when it has been built, oracle/_ref/, the
 reference's own serial executor and host helpers compiled from its headers.
-Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
-module, and only as the checker or the timed CPU baseline.
+Only tests/, __graft_entry__.smoke() and bench.py's CPU legs use this module,
+and only as the checker or the timed CPU baseline.
+
+liboracle.so also carries the workloads' seeded generator (compiled from the
+solver library's generator source) and b = A*ones, so the CPU legs make their
+inputs without loading the solver library; tests pin both to the solver
+library's output and to the reference's.
 """
 from __future__ import annotations
 
 import ctypes as C
+import importlib.util
 import subprocess
 from pathlib import Path
 
@@ -21,6 +27,29 @@ REFERENCE = Path("/root/reference")
 
 FORWARD, BACKWARD = 0, 1
 P = C.c_void_p
+GEN_SRC = HERE.parent / "capellinisptrsv_gb300" / "csrc" / "host" / "generate.c"
+WORKLOADS_PY = HERE.parent / "capellinisptrsv_gb300" / "workloads.py"
+
+
+class GenParams(C.Structure):
+    """capsp_gen_params_t (include/capsp.h)."""
+    _fields_ = [("n", C.c_int64), ("seed", C.c_uint64), ("stream", C.c_uint64), ("kind", C.c_int),
+                ("kmin", C.c_int), ("kmax", C.c_int), ("band", C.c_int64), ("zipf_s", C.c_double),
+                ("zipf_cap", C.c_int), ("near_window", C.c_int)]
+
+
+_W = None
+
+
+def workloads():
+    """The workload table (capellinisptrsv_gb300/workloads.py), loaded by path
+    so that the solver package, and with it its library, is not imported."""
+    global _W
+    if _W is None:
+        sp = importlib.util.spec_from_file_location("_capsp_workloads", WORKLOADS_PY)
+        _W = importlib.util.module_from_spec(sp)
+        sp.loader.exec_module(_W)
+    return _W
 
 
 def build(ref: bool | None = None) -> None:
@@ -43,7 +72,7 @@ _lib = None
 def lib() -> C.CDLL:
     global _lib
     if _lib is None:
-        src = [HERE / "oracle.c", HERE / "oracle_impl.h", HERE / "oracle.h"]
+        src = [HERE / "oracle.c", HERE / "oracle_impl.h", HERE / "oracle.h", GEN_SRC]
         if not LIB.exists() or any(s.stat().st_mtime > LIB.stat().st_mtime for s in src):
             build(ref=False)
         _lib = C.CDLL(str(LIB))
@@ -55,8 +84,15 @@ def lib() -> C.CDLL:
             getattr(_lib, f"oracle_grad_val_{t}").restype = None
             getattr(_lib, f"oracle_transpose_{t}").argtypes = [C.c_int, C.c_int, C.c_int, P, P, P, P, P, P]
             getattr(_lib, f"oracle_transpose_{t}").restype = None
+            getattr(_lib, f"oracle_get_x_b_{t}").argtypes = [C.c_int, P, P, P]
+            getattr(_lib, f"oracle_get_x_b_{t}").restype = None
         _lib.oracle_analyser.argtypes = [P, C.c_int, C.c_int, P]
         _lib.oracle_analyser.restype = None
+        _lib.capsp_gen_rowptr.argtypes = [C.POINTER(GenParams), P]
+        _lib.capsp_gen_fill_f64.argtypes = [C.POINTER(GenParams), P, P, P]
+        _lib.capsp_gen_normal_f64.argtypes = [C.c_uint64, C.c_uint64, C.c_int64, P]
+        _lib.capsp_digest.argtypes = [C.c_int, C.c_int, P, P, P, C.c_int]
+        _lib.capsp_digest.restype = C.c_uint64
     return _lib
 
 
@@ -139,6 +175,60 @@ def grad_val(rowptr, colidx, y, x) -> np.ndarray:
     out = np.empty(len(colidx), dtype=y.dtype)
     getattr(lib(), f"oracle_grad_val_{_t(y)}")(len(rowptr) - 1, _p(rowptr), _p(colidx), k, _p(y), _p(x), _p(out))
     return out
+
+
+def get_x_b(rowptr, val) -> np.ndarray:
+    """b = A * ones in the value type, row order (the reference's get_x_b)."""
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    val = np.ascontiguousarray(val)
+    b = np.empty(len(rowptr) - 1, dtype=val.dtype)
+    getattr(lib(), f"oracle_get_x_b_{_t(val)}")(len(b), _p(rowptr), _p(val), _p(b))
+    return b
+
+
+# ---------------------------------------------------------------------------
+# seeded inputs (the workloads' generator, built into liboracle.so)
+# ---------------------------------------------------------------------------
+
+def generate(workload=None, *, seed=0, stream=0, **params):
+    """(n, rowptr, colidx, val) of a workload, from the same seeded generator as
+    the solver library's ``generate``."""
+    sp = workloads().spec(workload, **params)
+    p = GenParams(int(sp["n"]), int(seed), int(stream), int(sp["kind"]), int(sp["kmin"]), int(sp["kmax"]),
+                  int(sp["band"]), float(sp["zipf_s"]), int(sp["zipf_cap"]), int(sp["near_window"]))
+    n = int(sp["n"])
+    rowptr = np.empty(n + 1, dtype=np.int32)
+    if lib().capsp_gen_rowptr(C.byref(p), _p(rowptr)) != 0:
+        raise ValueError("generator rejected the parameters")
+    colidx = np.empty(int(rowptr[-1]), dtype=np.int32)
+    val = np.empty(int(rowptr[-1]), dtype=np.float64)
+    if lib().capsp_gen_fill_f64(C.byref(p), _p(rowptr), _p(colidx), _p(val)) != 0:
+        raise ValueError("generator fill failed")
+    return n, rowptr, colidx, val
+
+
+def generate_batched(nsys=None, *, seed=0):
+    """(n, rowptr, colidx, val, sys_rowoff) of the batched workload."""
+    W = workloads()
+    d = dict(W.BATCH_DEFAULTS)
+    nsys = nsys or d["nsys"]
+    sizes = W.batched_sizes(nsys, seed, d["nmin"], d["nmax"])
+    parts = [generate(seed=seed, stream=s + 1, **W.batched_system_spec(sizes[s], d["kmin"], d["kmax"],
+                                                                       d["band_div"]))[1:]
+             for s in range(nsys)]
+    return W.assemble_batched(parts, sizes)
+
+
+def normal(count, *, seed=0, stream=0) -> np.ndarray:
+    out = np.empty(int(count), dtype=np.float64)
+    lib().capsp_gen_normal_f64(int(seed), int(stream), int(count), _p(out))
+    return out
+
+
+def digest(n, rowptr, colidx, val) -> int:
+    val = np.ascontiguousarray(val)
+    return int(lib().capsp_digest(int(n), len(colidx), _p(np.ascontiguousarray(rowptr, np.int32)),
+                                  _p(np.ascontiguousarray(colidx, np.int32)), _p(val), val.dtype.itemsize))
 
 
 # ---------------------------------------------------------------------------

@@ -35,6 +35,9 @@ void oracle_grad_val_f64(int n, const int *rowptr, const int *colidx, int rhs, c
 void oracle_grad_val_f32(int n, const int *rowptr, const int *colidx, int rhs, const float *y,
                          const float *x, float *grad);
 
+void oracle_get_x_b_f64(int m, const int *rowptr, const double *val, double *b);
+void oracle_get_x_b_f32(int m, const int *rowptr, const float *val, float *b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -124,3 +124,19 @@ void OSFX(oracle_grad_val)(int n, const int *rowptr, const int *colidx, int rhs,
             grad[k] = -acc;
         }
 }
+
+/* b = A * ones over the stored entries of each row, accumulated in row order
+ * in the value type: the known-answer right-hand side of get_x_b
+ * (CUDA/ourWrtFst/read_mtx.h:260-278, whose x_ref is all ones, so each
+ * product val * x_ref[col] is val itself). */
+void OSFX(oracle_get_x_b)(int m, const int *rowptr, const OVT *val, OVT *b)
+{
+    for (int i = 0; i < m; ++i) {
+        OVT acc = (OVT)0;
+        for (int j = rowptr[i]; j < rowptr[i + 1]; ++j) {
+            OVT prod = val[j] * (OVT)1;
+            acc = acc + prod;
+        }
+        b[i] = acc;
+    }
+}

@@ -107,3 +107,35 @@ def test_oracle_grad_val_definition():
     rows = np.repeat(np.arange(m.n), np.diff(m.rowptr))
     want = -np.sum(y[rows] * x[m.colidx], axis=1)
     assert np.allclose(got, want, rtol=1e-14, atol=1e-14)
+
+
+def test_oracle_generator_matches_library_and_golden(golden):
+    """The CPU legs generate their own inputs with liboracle's copy of the
+    generator: same digest as the solver library's, and as the fixture."""
+    n, rp, ci, v = oracle.generate("plain_20k", seed=0)
+    assert int(rp[-1]) == int(golden["plain_20k_nnz"][0])
+    assert oracle.digest(n, rp, ci, v) == int(golden["plain_20k_digest"][0])
+    for name, kw in [("wide_4m", dict(n=50_000)), ("zipf_1m", dict(n=30_000)), ("grad_1m", dict(n=40_000)),
+                     ("zipf40_1m", dict(n=5_000))]:
+        on, orp, oci, ov = oracle.generate(name, seed=0, **kw)
+        m = cs.generate(name, seed=0, **kw)
+        assert on == m.n and oracle.digest(on, orp, oci, ov) == m.digest(), name
+        assert np.array_equal(orp, m.rowptr) and np.array_equal(oci, m.colidx) and np.array_equal(ov, m.val)
+    assert np.array_equal(oracle.normal(1000, seed=0, stream=7), cs.normal(1000, seed=0, stream=7))
+
+
+def test_oracle_batched_generator_matches_library():
+    n, rp, ci, v, so = oracle.generate_batched(24, seed=0)
+    m = cs.generate_batched(24, seed=0)
+    assert n == m.n
+    for a, b in [(rp, m.rowptr), (ci, m.colidx), (v, m.val), (so, m.sys_rowoff)]:
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("t,dt", [("f64", np.float64), ("f32", np.float32)])
+def test_oracle_get_x_b_matches_reference(golden, t, dt):
+    m = cs.generate("plain_20k", seed=0)
+    val = m.val.astype(dt)
+    b = oracle.get_x_b(m.rowptr, val)
+    assert np.array_equal(sha(b), golden[f"plain_20k_b_{t}_sha"])
+    assert np.array_equal(b, cs.get_x_b(m.n, m.n, m.rowptr, m.colidx, val)[1])
