@@ -21,6 +21,7 @@ FMT_CSR, FMT_CSC = 0, 1
 LOWER, UPPER = 0, 1
 ALG_AUTO, ALG_WRTFST, ALG_TWOPART, ALG_MIX, ALG_SYNCFREE_CSC = range(5)
 SCHED_NATURAL, SCHED_LEVEL = 0, 1
+L2_HINTS, L2_WINDOW_AND_HINTS, L2_WINDOW = 0, 1, 2
 DEVICE_POINTERS, SKIP_VALIDATION = 0x1, 0x2
 GEN_UNIFORM_BAND, GEN_ZIPF_NEAR_FAR = 0, 1
 
@@ -73,6 +74,7 @@ _SIGS = {
     "capsp_destroy": (I, [H]),
     "capsp_get_info": (I, [H, C.POINTER(Info)]),
     "capsp_set_algorithm": (I, [H, I]),
+    "capsp_set_l2_policy": (I, [H, I]),
     "capsp_set_mix_border": (I, [H, I]),
     "capsp_set_schedule": (I, [H, I]),
     "capsp_set_tuning": (I, [H, I, I, I]),

@@ -143,6 +143,12 @@ struct capsp_handle_s {
     cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;
     unsigned long long *trace = nullptr;  // borrowed tracing buffer (2n entries)
     // level schedule of the row-driven view (positions, capsp_level_layout)
+    // L2 treatment of the publication vector (capsp_set_l2_policy)
+    int l2_mode = CAPSP_L2_HINTS;
+    bool l2_limit_set = false;
+    size_t l2_prev_limit = 0;  // persisting carve-out before this handle changed it
+    size_t l2_window = 0;      // largest window the device accepts
+    size_t l2_persist = 0;     // persisting carve-out this handle asked for
     int sched = CAPSP_SCHED_LEVEL;
     bool level_built = false;
     int levels = 0;
@@ -164,6 +170,8 @@ static void free_handle(capsp_handle_t h)
         return;
     DeviceGuard g(h->device);
     h->graphs.clear();
+    if (h->l2_limit_set)
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, h->l2_prev_limit);
     for (auto &kv : h->mix)
         cudaFree(kv.second.d);
     if (h->own_struct) {
@@ -534,6 +542,33 @@ extern "C" capsp_status_t capsp_set_backoff(capsp_handle_t h, unsigned sleep_max
     return CAPSP_OK;
 }
 
+extern "C" capsp_status_t capsp_set_l2_policy(capsp_handle_t h, int mode)
+{
+    if (!h || (mode != CAPSP_L2_HINTS && mode != CAPSP_L2_WINDOW_AND_HINTS && mode != CAPSP_L2_WINDOW))
+        return fail(CAPSP_ERR_INVALID, "need a handle and a capsp_l2_policy_t mode");
+    std::lock_guard<std::recursive_mutex> lk(h->mu);
+    DeviceGuard g(h->device);
+    if (mode != CAPSP_L2_HINTS && !h->l2_limit_set) {
+        int max_win = 0, max_persist = 0;
+        CAPSP_CUDA(cudaDeviceGetAttribute(&max_win, cudaDevAttrMaxAccessPolicyWindowSize, h->device));
+        CAPSP_CUDA(cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, h->device));
+        if (max_win <= 0 || max_persist <= 0)
+            return fail(CAPSP_ERR_UNSUPPORTED, "this device has no persisting L2 carve-out");
+        CAPSP_CUDA(cudaDeviceGetLimit(&h->l2_prev_limit, cudaLimitPersistingL2CacheSize));
+        const size_t want = h->vbytes * (size_t)h->n;
+        h->l2_persist = want < (size_t)max_persist ? want : (size_t)max_persist;
+        CAPSP_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, h->l2_persist));
+        h->l2_limit_set = true;
+        h->l2_window = (size_t)max_win;
+    } else if (mode == CAPSP_L2_HINTS && h->l2_limit_set) {
+        CAPSP_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, h->l2_prev_limit));
+        h->l2_limit_set = false;
+    }
+    h->l2_mode = mode;
+    h->graphs.invalidate();
+    return CAPSP_OK;
+}
+
 extern "C" capsp_status_t capsp_set_algorithm(capsp_handle_t h, int algorithm)
 {
     if (!h)
@@ -723,10 +758,14 @@ static capsp_status_t ensure_column_order(capsp_handle_t h, int backward)
 }
 
 // Launch shape of a row-path launch with nrhs right-hand sides.  Defaults
-// measured on GB300: with one lane per row (32 rows per warp) eight resident
-// warps per SM suit wide levels and two suit narrow ones (more rows in flight
-// than a few levels only add pollers); with G >= 4 lanes per row a warp holds
-// few rows, so every warp the SM can hold in 128-thread blocks pays off.
+// measured on GB300: with one lane per row (32 rows per warp) two resident
+// warps per SM suit narrow levels (more rows in flight than a few levels only
+// add pollers), twelve suit levels of 4k-32k rows (wide_4m, 5.8k rows per
+// level, warps per SM 2/4/6/8/12/16: 1.708/1.091/0.877/0.765/0.748/0.782 ms;
+// FP32 0.712 -> 0.694 ms at 12) and sixteen the levels of 32k rows and more,
+// which are bound by throughput (2,048 banded systems, 93k rows per level:
+// 2.95 ms at 8, 1.81 ms at 16); with G >= 4 lanes per row a warp holds few
+// rows, so every warp the SM can hold in 128-thread blocks pays off.
 // Wide levels with G >= 4 lanes per row also take the 64-register kernel build
 // (*cap), whatever the shape.
 // Levels of 32k rows and more on average keep the GPU busy without waiting on
@@ -747,7 +786,7 @@ static void row_shape(capsp_handle_t h, const Tuning &tn, int nrhs, int *block, 
     if (!tn.dflt)
         return;
     if (g == 1) {
-        *block = narrow ? 64 : 256;
+        *block = narrow ? 64 : (wide_levels(h) ? 512 : 384);
         *bps = 1;
     } else if (g == 2) {
         *block = 256;
@@ -865,6 +904,17 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs,
         a.wait = h->wait;
         a.stuck_row = h->stuck_row;
         a.trace = r0 == 0 ? h->trace : nullptr;
+        a.keep_hint = h->l2_mode != CAPSP_L2_WINDOW;
+        a.win_base = nullptr;
+        a.win_bytes = 0;
+        a.win_hit = 0.f;
+        if (level && h->l2_mode != CAPSP_L2_HINTS && h->l2_window > 0) {
+            const size_t bytes = h->vbytes * (size_t)h->n * (size_t)nb;
+            a.win_base = h->d_xp;
+            a.win_bytes = bytes < h->l2_window ? bytes : h->l2_window;
+            const double hit = (double)h->l2_persist / (double)a.win_bytes;
+            a.win_hit = hit >= 1.0 ? 1.f : (float)hit;
+        }
         const bool prof = h->profiling && r0 == 0;
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k0, st));

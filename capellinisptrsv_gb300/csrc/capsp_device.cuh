@@ -96,6 +96,13 @@ __device__ __forceinline__ unsigned long long l2_policy_evict_last()
     return p;
 }
 
+__device__ __forceinline__ unsigned long long l2_policy_evict_normal()
+{
+    unsigned long long p;
+    asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
 // read-only streamed loads with an L2 policy
 __device__ __forceinline__ int ld_stream(const int *p, unsigned long long pol)
 {

@@ -46,6 +46,12 @@ struct RowArgs {
     WaitCfg wait;
     int stuck_row;  // debug: this row never publishes (-1: none)
     unsigned long long *trace;  // tracing, per row i: [4i] chunk taken, [4i+1] first poll, [4i+2] last dependency received, [4i+3] published (ns)
+    int keep_hint;  // publication vector polled and stored with evict_last (1) or evict_normal (0)
+    // host side: an access-policy window (persisting) over the publication
+    // vector for this launch; win_bytes == 0: none
+    void *win_base;
+    size_t win_bytes;
+    float win_hit;
 };
 
 // Arguments of the column-driven solve (SyncFree CSC kernel, and the

@@ -722,7 +722,7 @@ __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const Row
     const int rl = lane / G, g = lane % G;
     L2Pol pol;
     pol.stream = l2_policy_evict_first();
-    pol.keep = l2_policy_evict_last();
+    pol.keep = a.keep_hint ? l2_policy_evict_last() : l2_policy_evict_normal();
     for (;;) {
         unsigned tk = 0, stop = 0;
         if (lane == 0) {
@@ -801,8 +801,25 @@ static cudaError_t launch_row_impl(const RowArgs<T> &a, int block, int bps, int 
         grid = need;
     if (grid < 1)
         grid = 1;
-    kern<<<(unsigned)grid, block, smem, st>>>(a);
-    return cudaGetLastError();
+    if (a.win_bytes == 0) {
+        kern<<<(unsigned)grid, block, smem, st>>>(a);
+        return cudaGetLastError();
+    }
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+    attr[0].val.accessPolicyWindow.base_ptr = a.win_base;
+    attr[0].val.accessPolicyWindow.num_bytes = a.win_bytes;
+    attr[0].val.accessPolicyWindow.hitRatio = a.win_hit;
+    attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, a);
 }
 
 // one lane per row on the level schedule, entries staged in shared memory

@@ -238,6 +238,12 @@ class TriangularSolver:
         """'level' (rows sorted by dependency level, the default) or 'natural' (row order)."""
         N.check(N.lib.capsp_set_schedule(self._h, {"natural": N.SCHED_NATURAL, "level": N.SCHED_LEVEL}[schedule]))
 
+    def set_l2_policy(self, mode: str) -> None:
+        """'hints' (default), 'window+hints' or 'window': L2 treatment of the
+        publication vector the dependency polls read (capsp_set_l2_policy)."""
+        code = {"hints": N.L2_HINTS, "window+hints": N.L2_WINDOW_AND_HINTS, "window": N.L2_WINDOW}[mode]
+        N.check(N.lib.capsp_set_l2_policy(self._h, code))
+
     def set_mix_border(self, border: int) -> None:
         N.check(N.lib.capsp_set_mix_border(self._h, int(border)))
 

@@ -89,6 +89,14 @@ typedef enum capsp_schedule {
     CAPSP_SCHED_LEVEL = 1    /* rows sorted by dependency level, built at analysis (default) */
 } capsp_schedule_t;
 
+/* L2 treatment of the position-ordered publication vector that every
+ * dependency poll reads (capsp_set_l2_policy). */
+typedef enum capsp_l2_policy {
+    CAPSP_L2_HINTS = 0,            /* polls and publications carry evict_last hints (default) */
+    CAPSP_L2_WINDOW_AND_HINTS = 1, /* plus a persisting access-policy window over the vector */
+    CAPSP_L2_WINDOW = 2            /* the window alone (evict_normal polls) */
+} capsp_l2_policy_t;
+
 /* capsp_analyse flags */
 #define CAPSP_DEVICE_POINTERS 0x1u /* ptr/idx/val are device pointers; the handle borrows them */
 #define CAPSP_SKIP_VALIDATION 0x2u /* trust the structure (no host/device structure check) */
@@ -159,6 +167,14 @@ capsp_status_t capsp_refresh_values(capsp_handle_t h, const void *val, void *str
 capsp_status_t capsp_destroy(capsp_handle_t h);
 
 capsp_status_t capsp_get_info(capsp_handle_t h, capsp_info_t *info);
+
+/* L2 treatment of the publication vector of level-schedule row solves
+ * (capsp_l2_policy_t).  The window modes reserve a persisting L2 carve-out of
+ * up to the vector's size (cudaLimitPersistingL2CacheSize, a setting of the
+ * calling process's context) and attach an access-policy window to each solve
+ * launch; returning to CAPSP_L2_HINTS or destroying the handle restores the
+ * carve-out the process had before.  The default needs neither. */
+capsp_status_t capsp_set_l2_policy(capsp_handle_t h, int mode);
 
 /* Choose the row-driven algorithm for CSR handles (capsp_algorithm_t). */
 capsp_status_t capsp_set_algorithm(capsp_handle_t h, int algorithm);

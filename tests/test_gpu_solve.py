@@ -398,3 +398,18 @@ def test_level_schedule_reports_levels(plain20k):
     info = s.info()
     assert info["schedule"] == 1
     assert info["levels"] == cs.matrix_layer(m.n, m.n, m.nnz, m.rowptr, m.colidx)[0]
+
+
+def test_l2_policy_modes_bit_identical(plain20k):
+    """The L2 policy changes caching only: the three modes give the same bits,
+    and leaving the window modes restores the process's persisting carve-out."""
+    m = plain20k
+    _, b = cs.get_x_b(m.n, m.n, m.rowptr, m.colidx, m.val)
+    s = solver_for(m)
+    bd = dev(b)
+    ref = host(s.solve(bd))
+    for mode in ("window+hints", "window", "hints"):
+        s.set_l2_policy(mode)
+        assert np.array_equal(host(s.solve(bd)), ref), mode
+    s.status()
+    assert rel_inf_err(ref, oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)) <= TOL64
