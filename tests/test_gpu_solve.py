@@ -7,6 +7,8 @@ All calls go through the C-ABI (capellinisptrsv_gb300 binds it with ctypes).
 """
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -413,3 +415,53 @@ def test_l2_policy_modes_bit_identical(plain20k):
         assert np.array_equal(host(s.solve(bd)), ref), mode
     s.status()
     assert rel_inf_err(ref, oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)) <= TOL64
+
+
+def _two_wide_levels(n=200_000, seed=5):
+    """Rows < n/2 have no dependencies; row i >= n/2 depends on i - n/2 - 7
+    (when that exists) and i - n/2: two levels of n/2 rows, the wide-level
+    launch shape (levels of 32k rows and more: 16 warps per SM)."""
+    rng = np.random.default_rng(seed)
+    h = n // 2
+    i = np.arange(n)
+    far = (i >= h + 7)
+    near = (i >= h)
+    cnt = 1 + far + near
+    rp = np.zeros(n + 1, np.int64)
+    rp[1:] = np.cumsum(cnt)
+    ci = np.empty(rp[-1], np.int32)
+    v = np.empty(rp[-1])
+    off1 = rng.uniform(-1, 1, n)
+    off2 = rng.uniform(-1, 1, n)
+    k = rp[:-1].copy()
+    ci[k[far]] = i[far] - h - 7
+    v[k[far]] = off1[far]
+    k[far] += 1
+    ci[k[near]] = i[near] - h
+    v[k[near]] = off2[near]
+    k[near] += 1
+    ci[k] = i
+    v[k] = 1.0 + np.where(far, np.abs(off1), 0.0) + np.where(near, np.abs(off2), 0.0)
+    return cs.CSRMatrix(n, rp.astype(np.int32), ci, v)
+
+
+@pytest.mark.parametrize("k,ld", [(1, 1), (3, 5), (16, 16), (40, 41)])
+def test_wide_levels_strided_multi_block_rhs(k, ld):
+    """Two levels of 100k rows: strided right-hand sides, several 32-RHS
+    blocks (k = 40), and columns past nrhs left untouched."""
+    m = _two_wide_levels()
+    s = solver_for(m)
+    assert s.info()["levels"] == 2
+    rng = np.random.default_rng(k)
+    b = np.zeros((m.n, ld))
+    b[:, :k] = rng.standard_normal((m.n, k))
+    bd = dev(b)
+    xd = torch.full_like(bd, 7.0)
+    N = cs._native
+    N.check(N.lib.capsp_solve(s._h, C.c_void_p(bd.data_ptr()), C.c_void_p(xd.data_ptr()), k, ld,
+                              C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    s.status()
+    x = host(xd)
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, np.ascontiguousarray(b[:, :k]))
+    assert rel_inf_err(x[:, :k].reshape(m.n, k), xo.reshape(m.n, k)) <= TOL64
+    assert np.all(x[:, k:] == 7.0)  # columns past nrhs untouched
