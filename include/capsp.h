@@ -173,7 +173,9 @@ capsp_status_t capsp_get_info(capsp_handle_t h, capsp_info_t *info);
  * up to the vector's size (cudaLimitPersistingL2CacheSize, a setting of the
  * calling process's context) and attach an access-policy window to each solve
  * launch; returning to CAPSP_L2_HINTS or destroying the handle restores the
- * carve-out the process had before.  The default needs neither. */
+ * carve-out value this handle found when it first changed it (handles that
+ * change it concurrently restore in their own order).  The default needs
+ * neither. */
 capsp_status_t capsp_set_l2_policy(capsp_handle_t h, int mode);
 
 /* Choose the row-driven algorithm for CSR handles (capsp_algorithm_t). */
