@@ -887,7 +887,7 @@ def measure_autograd(args, cpu_seconds):
         x = cs.sptrsv(solver, val, b_in)
         loss = 0.5 * ((x - xs_in) ** 2).sum()
         loss.backward()
-        return float(loss)
+        return float(loss.detach())
 
     e2e_step()
     reps = max(3, min(args.steps, 20))

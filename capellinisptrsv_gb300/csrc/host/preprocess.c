@@ -169,13 +169,43 @@ int capsp_row_levels(int n, const int *rowptr, const int *colidx, int *level, in
  * columns of a CSC read as rows of the transpose).  Solve order visits rows
  * 0..n-1 (diagonal last, dependencies on smaller rows) or, with upper != 0,
  * rows n-1..0 (diagonal first, dependencies on larger rows).  Every row gets
- * level 1 + the deepest level among its dependencies; a counting sort by
- * level, then by dependency count (descending) inside each level, gives
- * order[k] (k-th row to solve) and position[row] = k.  Any order that lists
- * dependencies first keeps the sync-free solve correct; this one puts rows
- * that become ready together, and need as many passes, next to each other.
+ * level 1 + the deepest level among its dependencies, and the levels are laid
+ * out one after another, giving order[k] (k-th row to solve) and
+ * position[row] = k.  Any order that lists dependencies first keeps the
+ * sync-free solve correct.  Inside a level, rows are ordered
+ *   - in a level that holds a row of more than CAPSP_ROW_PASS dependencies
+ *     (more than the row kernel takes in one pass), by dependency count, most
+ *     first (counts of 63 and more share a bucket), then solve order: a warp's
+ *     32 consecutive rows then need the same number of passes instead of all
+ *     waiting for the longest (measured on GB300: 2,048 banded systems with
+ *     3-12 dependencies per row, 1.96 -> 1.64 ms; 1M rows with 2-10, 1.38 ->
+ *     1.35 ms);
+ *   - in any other level, by the position of the row's newest dependency (the
+ *     last to be published, as a rule), then solve order: a warp's 32 rows then
+ *     wait on a few neighbouring rows of the previous level, published by one
+ *     or two warps, so their polls share cache lines instead of reaching 32
+ *     unrelated producers (measured on GB300: wide_4m 0.756 -> 0.742 ms, FP32
+ *     0.694 -> 0.671 ms; applied to the multi-pass levels too, it cost the
+ *     2,048 systems 1.4 % and 1M rows with 2-10 dependencies 1 %).
  * level_start (n+2 ints, optional) receives the first position of every level.
  * Returns the number of levels, or -1 on allocation failure. */
+typedef struct {
+    int bucket; /* 0 unless the level is sorted by dependency count: 63 - min(count, 63) */
+    int key;    /* levels sorted by dependency count: 0; others: position of the newest dependency (-1: none) */
+    int rank;   /* solve order inside the level */
+    int row;
+} sched_item_t;
+
+static int cmp_sched(const void *pa, const void *pb)
+{
+    const sched_item_t *a = (const sched_item_t *)pa, *b = (const sched_item_t *)pb;
+    if (a->bucket != b->bucket)
+        return a->bucket < b->bucket ? -1 : 1;
+    if (a->key != b->key)
+        return a->key < b->key ? -1 : 1;
+    return a->rank < b->rank ? -1 : (a->rank > b->rank);
+}
+
 int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *order, int *position,
                          int *level_start)
 {
@@ -202,9 +232,11 @@ int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *
             deepest = lv;
     }
     /* exclusive scan over levels 1..deepest: first position of each level */
-    int run = 0;
+    int run = 0, widest = 0;
     for (int l = 0; l <= deepest + 1; ++l) {
         int c = cnt[l];
+        if (c > widest)
+            widest = c;
         cnt[l] = run;
         run += c;
     }
@@ -216,43 +248,47 @@ int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *
         const int k = cnt[lev[p]]++;
         order[k] = i;
     }
-    /* Within a level that holds a row of more than CAPSP_ROW_PASS
-     * dependencies (more than the row kernel takes in one pass), rows with
-     * more dependencies come first (counts of 63 and more share a bucket;
-     * ties keep solve order).  A warp's 32 consecutive rows then need the
-     * same number of passes instead of all waiting for the longest (measured
-     * on GB300: 2,048 banded systems with 3-12 dependencies per row, 1.96 ->
-     * 1.64 ms; 1M rows with 2-10, 1.38 -> 1.35 ms).  A level whose rows all
-     * fit one pass keeps solve order, which keeps neighbouring rows' b and x
-     * close together (4M rows with 1-7 dependencies: 0.80 ms kept, 0.81 ms
-     * sorted). */
-    int *tmp = lev; /* the row levels are no longer needed */
+    sched_item_t *items = (sched_item_t *)malloc(sizeof(sched_item_t) * (size_t)(widest > 0 ? widest : 1));
+    if (!items) {
+        free(lev);
+        free(cnt);
+        return -1;
+    }
+    /* levels in order: the positions of every earlier level are final when a
+     * level's rows are keyed by their newest dependency */
     for (int l = 1; l <= deepest; ++l) {
         /* cnt[l] now holds the end of level l, cnt[l - 1] its start */
         const int a = cnt[l - 1], b = cnt[l];
-        if (b - a < 2)
-            continue;
-        int start[65] = {0}; /* bucket 0: 63+ dependencies ... bucket 63: none */
         int most = 0;
         for (int k = a; k < b; ++k) {
             const int i = order[k];
             const int d = ptr[i + 1] - ptr[i] - 1;
-            start[64 - (d < 63 ? d : 63)]++;
             most = d > most ? d : most;
         }
-        if (most <= CAPSP_ROW_PASS)
-            continue;
-        for (int t = 1; t < 65; ++t)
-            start[t] += start[t - 1];
+        const int by_count = most > CAPSP_ROW_PASS;
         for (int k = a; k < b; ++k) {
             const int i = order[k];
-            const int d = ptr[i + 1] - ptr[i] - 1;
-            tmp[a + start[63 - (d < 63 ? d : 63)]++] = i;
+            const int s = ptr[i] + (upper ? 1 : 0), e = ptr[i + 1] - (upper ? 0 : 1);
+            int key = -1;
+            if (!by_count)
+                for (int j = s; j < e; ++j)
+                    if (position[idx[j]] > key)
+                        key = position[idx[j]];
+            const int d = e - s;
+            sched_item_t *it = &items[k - a];
+            it->bucket = by_count ? 63 - (d < 63 ? d : 63) : 0;
+            it->key = key;
+            it->rank = k - a;
+            it->row = i;
         }
-        memcpy(order + a, tmp + a, sizeof(int) * (size_t)(b - a));
+        if (b - a > 1)
+            qsort(items, (size_t)(b - a), sizeof(sched_item_t), cmp_sched);
+        for (int k = a; k < b; ++k) {
+            order[k] = items[k - a].row;
+            position[order[k]] = k;
+        }
     }
-    for (int k = 0; k < n; ++k)
-        position[order[k]] = k;
+    free(items);
     free(lev);
     free(cnt);
     return deepest;

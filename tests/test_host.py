@@ -213,20 +213,23 @@ def test_level_schedule_is_a_topological_level_order(upper):
     lev_of_pos = np.repeat(np.arange(1, levels + 1), np.diff(start[1:levels + 2]))
     assert np.all(np.diff(lev_of_pos) >= 0)
     # inside a level holding a row of more than 8 dependencies (one pass of the
-    # row kernel): dependency count non-increasing (63+ in one bucket), ties in
-    # solve order; any other level keeps solve order
+    # row kernel): dependency count non-increasing (63+ in one bucket), then
+    # solve order; inside any other level: the position of the newest
+    # dependency, then solve order
     ndep = np.minimum(np.diff(rp)[order] - 1, 63)
     solve_rank = (m.n - 1 - order) if upper else order
+    newest = np.array([dep_idx[dep_ptr[k]:dep_ptr[k + 1]].max() if dep_ptr[k + 1] > dep_ptr[k] else -1
+                       for k in range(m.n)])
     sorted_levels = 0
     for l in range(1, levels + 1):
         a, b = start[l], start[l + 1]
-        d, r = ndep[a:b], solve_rank[a:b]
-        if d.size and d.max() > 8:
-            sorted_levels += 1
-            assert np.all(np.diff(d) <= 0)
-            assert np.all((np.diff(d) < 0) | (np.diff(r) > 0))
-        else:
-            assert np.all(np.diff(r) > 0)
+        d, key, r = ndep[a:b], newest[a:b], solve_rank[a:b]
+        multi = bool(d.size and d.max() > 8)
+        sorted_levels += multi
+        bucket = -d if multi else np.zeros_like(d)
+        key = np.zeros_like(key) if multi else key
+        triples = list(zip(bucket.tolist(), key.tolist(), r.tolist()))
+        assert triples == sorted(triples)
     assert 0 < sorted_levels < levels
 
 
