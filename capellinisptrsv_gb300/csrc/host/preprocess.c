@@ -189,23 +189,6 @@ int capsp_row_levels(int n, const int *rowptr, const int *colidx, int *level, in
  *     2,048 systems 1.4 % and 1M rows with 2-10 dependencies 1 %).
  * level_start (n+2 ints, optional) receives the first position of every level.
  * Returns the number of levels, or -1 on allocation failure. */
-typedef struct {
-    int bucket; /* 0 unless the level is sorted by dependency count: 63 - min(count, 63) */
-    int key;    /* levels sorted by dependency count: 0; others: position of the newest dependency (-1: none) */
-    int rank;   /* solve order inside the level */
-    int row;
-} sched_item_t;
-
-static int cmp_sched(const void *pa, const void *pb)
-{
-    const sched_item_t *a = (const sched_item_t *)pa, *b = (const sched_item_t *)pb;
-    if (a->bucket != b->bucket)
-        return a->bucket < b->bucket ? -1 : 1;
-    if (a->key != b->key)
-        return a->key < b->key ? -1 : 1;
-    return a->rank < b->rank ? -1 : (a->rank > b->rank);
-}
-
 int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *order, int *position,
                          int *level_start)
 {
@@ -248,47 +231,71 @@ int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *
         const int k = cnt[lev[p]]++;
         order[k] = i;
     }
-    sched_item_t *items = (sched_item_t *)malloc(sizeof(sched_item_t) * (size_t)(widest > 0 ? widest : 1));
-    if (!items) {
+    /* Stable counting sorts inside each level, levels in order (the positions
+     * of every earlier level are final when a level's rows are keyed).  A
+     * row's newest dependency always lies in the previous level (its deepest
+     * dependency sets its level, and positions ascend with the level), so the
+     * key of a single-pass level ranges over the previous level's positions. */
+    int *tmp = lev; /* the row levels are no longer needed */
+    int *hist = (int *)malloc(sizeof(int) * ((size_t)(widest > 64 ? widest : 64) + 1));
+    int *key = (int *)malloc(sizeof(int) * (size_t)(widest > 0 ? widest : 1));
+    if (!hist || !key) {
+        free(hist);
+        free(key);
         free(lev);
         free(cnt);
         return -1;
     }
-    /* levels in order: the positions of every earlier level are final when a
-     * level's rows are keyed by their newest dependency */
     for (int l = 1; l <= deepest; ++l) {
         /* cnt[l] now holds the end of level l, cnt[l - 1] its start */
         const int a = cnt[l - 1], b = cnt[l];
-        int most = 0;
-        for (int k = a; k < b; ++k) {
-            const int i = order[k];
-            const int d = ptr[i + 1] - ptr[i] - 1;
-            most = d > most ? d : most;
+        if (b - a > 1) {
+            int most = 0;
+            for (int k = a; k < b; ++k) {
+                const int i = order[k];
+                const int d = ptr[i + 1] - ptr[i] - 1;
+                most = d > most ? d : most;
+            }
+            int base = 0, range;
+            if (most > CAPSP_ROW_PASS) {
+                /* bucket 0: 63+ dependencies ... bucket 63: none */
+                range = 64;
+                for (int k = a; k < b; ++k) {
+                    const int i = order[k];
+                    const int d = ptr[i + 1] - ptr[i] - 1;
+                    key[k - a] = 63 - (d < 63 ? d : 63);
+                }
+            } else if (l > 1) {
+                base = cnt[l - 2];
+                range = a - base; /* the previous level's positions */
+                for (int k = a; k < b; ++k) {
+                    const int i = order[k];
+                    const int s = ptr[i] + (upper ? 1 : 0), e = ptr[i + 1] - (upper ? 0 : 1);
+                    int newest = base;
+                    for (int j = s; j < e; ++j)
+                        if (position[idx[j]] > newest)
+                            newest = position[idx[j]];
+                    key[k - a] = newest - base;
+                }
+            } else {
+                range = 0; /* level 1: no dependencies, solve order */
+            }
+            if (range > 0) {
+                memset(hist, 0, sizeof(int) * ((size_t)range + 1));
+                for (int k = a; k < b; ++k)
+                    hist[key[k - a] + 1]++;
+                for (int t = 0; t < range; ++t)
+                    hist[t + 1] += hist[t];
+                for (int k = a; k < b; ++k)
+                    tmp[a + hist[key[k - a]]++] = order[k];
+                memcpy(order + a, tmp + a, sizeof(int) * (size_t)(b - a));
+            }
         }
-        const int by_count = most > CAPSP_ROW_PASS;
-        for (int k = a; k < b; ++k) {
-            const int i = order[k];
-            const int s = ptr[i] + (upper ? 1 : 0), e = ptr[i + 1] - (upper ? 0 : 1);
-            int key = -1;
-            if (!by_count)
-                for (int j = s; j < e; ++j)
-                    if (position[idx[j]] > key)
-                        key = position[idx[j]];
-            const int d = e - s;
-            sched_item_t *it = &items[k - a];
-            it->bucket = by_count ? 63 - (d < 63 ? d : 63) : 0;
-            it->key = key;
-            it->rank = k - a;
-            it->row = i;
-        }
-        if (b - a > 1)
-            qsort(items, (size_t)(b - a), sizeof(sched_item_t), cmp_sched);
-        for (int k = a; k < b; ++k) {
-            order[k] = items[k - a].row;
+        for (int k = a; k < b; ++k)
             position[order[k]] = k;
-        }
     }
-    free(items);
+    free(hist);
+    free(key);
     free(lev);
     free(cnt);
     return deepest;
