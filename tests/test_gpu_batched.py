@@ -123,3 +123,29 @@ def test_graph_solve_csc_first_call():
     st.synchronize()
     s.status(st)
     assert rel_inf_err(x.cpu().numpy(), oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)) <= 1e-12
+
+
+def test_graph_cache_after_value_repointing():
+    """Natural schedule: a captured solve reads the value array itself, so
+    re-pointing the handle at new values must drop the cached graph (a stale
+    replay would solve with the old values)."""
+    m = cs.generate("plain_20k", seed=0)
+    s = cs.TriangularSolver(t(m.rowptr), t(m.colidx), t(m.val), schedule="natural")
+    b = np.random.default_rng(5).standard_normal(m.n)
+    bd, x = t(b), torch.empty(m.n, dtype=torch.float64, device=DEV)
+    st = torch.cuda.Stream()
+    with torch.cuda.stream(st):
+        s.graph_solve(bd, x, st)
+    st.synchronize()
+    assert s.info()["cached_graphs"] == 1
+    val2 = m.val * 1.5  # same structure, scaled values (still diagonally dominant)
+    v2 = t(val2)
+    s.refresh_values(v2)
+    torch.cuda.synchronize()
+    assert s.info()["cached_graphs"] == 0
+    with torch.cuda.stream(st):
+        s.graph_solve(bd, x, st)
+    s.status(st)
+    assert rel_inf_err(x.cpu().numpy(), oracle.solve_csr_lower(m.rowptr, m.colidx, val2, b)) <= 1e-12
+    s.set_schedule("level")
+    assert s.info()["cached_graphs"] == 0
