@@ -1,9 +1,12 @@
 """Differentiable sparse triangular solve: x = L^{-1} b as a torch.autograd.Function.
 
-Forward runs the row-driven sync-free solve.  Backward is hand-written: one
-column-driven sync-free sweep over the SAME CSR arrays solves L^T y = g
-(grad_b = y; no transpose is built) and, fused into it, writes
-grad_val[k] = -sum_r y[row_k, r] * x[col_k, r] for every stored entry k.
+Forward runs the row-driven sync-free solve.  Backward is hand-written: the
+same row kernels over the solver's transposed copy of the structure (built
+once, its entries pointing back into the CSR values) solve L^T y = g
+(grad_b = y), then one pass writes grad_val[k] = -sum_r y[row_k, r] *
+x[col_k, r] for every stored entry k, each sum over the right-hand sides an
+FMA chain in one thread.  A solver set to "syncfree_csc" runs the backward
+column-driven on the CSR arrays instead, with grad_val fused into the sweep.
 """
 from __future__ import annotations
 

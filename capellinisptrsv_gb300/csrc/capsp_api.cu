@@ -79,6 +79,27 @@ struct MixTable {
 void destroy_graph_exec(cudaGraphExec_t e) { cudaGraphExecDestroy(e); }
 typedef GraphCache<cudaGraphExec_t, destroy_graph_exec> Graphs;
 
+// Level schedule of one row-driven view of the matrix (capsp_level_layout):
+// view 0 reads the stored arrays as rows (CSR rows; CSC columns, i.e. rows of
+// the transpose), view 1 their transpose, built on the host from the stored
+// structure.  Entries and diagonals keep their index into the stored values
+// (d_lsrc, d_dsrc), so one value array serves both views.
+struct RowView {
+    bool built = false;
+    int upper = 0;        // its rows are upper-triangular (diagonal first)
+    int levels = 0;
+    bool narrow = false;  // levels narrower than ~4k rows on average
+    int *d_perm = nullptr, *d_lptr = nullptr, *d_lidx = nullptr, *d_lsrc = nullptr, *d_dsrc = nullptr;
+    void *d_lval = nullptr, *d_linv = nullptr;
+    std::vector<int> h_lcum;  // lptr[k] + k: row-count prefix in position space (mix tables)
+};
+
+// Which operations a handle solves through which view: the plain solve of a
+// CSR handle and the transpose of a CSC handle walk the stored arrays as rows
+// (view 0); the other two walk the transposed view (view 1), or, under
+// CAPSP_ALG_SYNCFREE_CSC, the stored arrays column by column.
+enum Op { kOpSolve, kOpTranspose, kOpTransposeGrad };
+
 struct DeviceGuard {
     int prev = -1;
     explicit DeviceGuard(int dev)
@@ -126,10 +147,7 @@ struct capsp_handle_s {
     // warps per SM; more resident warps only add pollers
     Tuning tune = {kRowWrtFst, 1, 256, 1, 10};
     bool tune_explicit = false;
-    // levels narrower than ~4k rows: two resident warps per SM for the row
-    // path by default (more rows in flight than a few levels only add pollers)
-    bool narrow_levels = false;
-    std::map<int, Tuning> tuned;
+    std::map<int, Tuning> tuned;  // autotuned plain solves, by nrhs
     // no nanosleep backoff by default: measured neutral on wide levels and
     // 7 % faster on deep chains (zipf_1m), where it delays each detection
     WaitCfg wait = {10000000000ull, 1u << 30, 0u};
@@ -142,20 +160,15 @@ struct capsp_handle_s {
     bool profiling = false;
     cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;
     unsigned long long *trace = nullptr;  // borrowed tracing buffer (2n entries)
-    // level schedule of the row-driven view (positions, capsp_level_layout)
     // L2 treatment of the publication vector (capsp_set_l2_policy)
     int l2_mode = CAPSP_L2_HINTS;
     bool l2_limit_set = false;
     size_t l2_prev_limit = 0;  // persisting carve-out before this handle changed it
     size_t l2_window = 0;      // largest window the device accepts
     size_t l2_persist = 0;     // persisting carve-out this handle asked for
-    int sched = CAPSP_SCHED_LEVEL;
-    bool level_built = false;
-    int levels = 0;
-    int *d_perm = nullptr, *d_lptr = nullptr, *d_lidx = nullptr, *d_lsrc = nullptr, *d_dsrc = nullptr;
-    void *d_lval = nullptr, *d_linv = nullptr;
-    std::vector<int> h_lcum;  // lptr[k] + k: row-count prefix in position space (mix tables)
-    void *d_xp = nullptr;     // position-ordered publication scratch
+    int sched = CAPSP_SCHED_LEVEL;  // schedule of view 0; view 1 is always level-ordered
+    RowView view[2];
+    void *d_xp = nullptr;     // position-ordered publication scratch (both views)
     int xp_cap = 0;           // right-hand sides it holds
     int nsys = 0;
     std::vector<int> sys_rowoff;
@@ -188,13 +201,15 @@ static void free_handle(capsp_handle_t h)
     cudaFree(h->d_corder[1]);
     cudaFree(h->d_left);
     cudaFree(h->d_stage);
-    cudaFree(h->d_perm);
-    cudaFree(h->d_lptr);
-    cudaFree(h->d_lidx);
-    cudaFree(h->d_lsrc);
-    cudaFree(h->d_dsrc);
-    cudaFree(h->d_lval);
-    cudaFree(h->d_linv);
+    for (RowView &rv : h->view) {
+        cudaFree(rv.d_perm);
+        cudaFree(rv.d_lptr);
+        cudaFree(rv.d_lidx);
+        cudaFree(rv.d_lsrc);
+        cudaFree(rv.d_dsrc);
+        cudaFree(rv.d_lval);
+        cudaFree(rv.d_linv);
+    }
     cudaFree(h->d_xp);
     if (h->stage_stream)
         cudaStreamDestroy(h->stage_stream);
@@ -232,77 +247,145 @@ static capsp_status_t refresh_inv_diag(capsp_handle_t h)
     return CAPSP_OK;
 }
 
-// level-schedule values from the handle's current values, on `st`
-static capsp_status_t launch_level_refresh(capsp_handle_t h, int *bad, cudaStream_t st)
+// level-schedule values of one built view from the handle's current values, on `st`
+static capsp_status_t launch_view_refresh(capsp_handle_t h, const RowView &rv, int *bad, cudaStream_t st)
 {
-    if (!h->level_built)
+    if (!rv.built)
         return CAPSP_OK;
     if (h->dtype == CAPSP_R_64F)
-        CAPSP_CUDA(launch_level_values<double>(h->d_lptr, h->d_lsrc, h->d_dsrc, h->n, (const double *)h->d_val,
-                                               (double *)h->d_lval, (double *)h->d_linv, bad, st));
+        CAPSP_CUDA(launch_level_values<double>(rv.d_lptr, rv.d_lsrc, rv.d_dsrc, h->n, (const double *)h->d_val,
+                                               (double *)rv.d_lval, (double *)rv.d_linv, bad, st));
     else
-        CAPSP_CUDA(launch_level_values<float>(h->d_lptr, h->d_lsrc, h->d_dsrc, h->n, (const float *)h->d_val,
-                                              (float *)h->d_lval, (float *)h->d_linv, bad, st));
+        CAPSP_CUDA(launch_level_values<float>(rv.d_lptr, rv.d_lsrc, rv.d_dsrc, h->n, (const float *)h->d_val,
+                                              (float *)rv.d_lval, (float *)rv.d_linv, bad, st));
     return CAPSP_OK;
 }
 
-// row-driven view of the handle: CSR rows in solve order, or CSC columns read
-// as rows of the transpose
+// ... of every built view
+static capsp_status_t launch_level_refresh(capsp_handle_t h, int *bad, cudaStream_t st)
+{
+    for (const RowView &rv : h->view)
+        CAPSP_TRY(launch_view_refresh(h, rv, bad, st));
+    return CAPSP_OK;
+}
+
+// view 0: CSR rows in solve order, or CSC columns read as rows of the transpose
 static int row_view_upper(capsp_handle_t h)
 {
     return h->format == CAPSP_FMT_CSR ? (h->uplo == CAPSP_UPPER) : (h->uplo == CAPSP_LOWER);
 }
 
-// Build the level schedule of the row-driven view (host work O(nnz) plus one
-// upload); synchronous.
-static capsp_status_t build_level(capsp_handle_t h)
+// the view an operation walks (when it is row-driven)
+static int view_of(capsp_handle_t h, Op op) { return (h->format == CAPSP_FMT_CSR) == (op == kOpSolve) ? 0 : 1; }
+
+// whether an operation runs column-driven on the stored arrays
+static bool column_driven(capsp_handle_t h, Op op) { return view_of(h, op) == 1 && h->alg == CAPSP_ALG_SYNCFREE_CSC; }
+
+// whether a view's solves follow its level schedule (view 1 has no other)
+static bool view_level(capsp_handle_t h, int v) { return v == 1 || h->sched == CAPSP_SCHED_LEVEL; }
+
+// The stored structure transposed by a counting sort over idx.  Each new row
+// lists its entries in stored-row order, so its diagonal comes first when the
+// stored rows are lower-triangular and last when they are upper-triangular,
+// as the transposed view needs; src[p] is the stored index of new entry p.
+static capsp_status_t transpose_structure(int n, int nnz, const int *ptr, const int *idx, std::vector<int> &tptr,
+                                          std::vector<int> &tidx, std::vector<int> &src)
 {
-    if (h->level_built)
+    tptr.assign((size_t)n + 1, 0);
+    tidx.resize((size_t)nnz);
+    src.resize((size_t)nnz);
+    for (int k = 0; k < nnz; ++k) {
+        if (idx[k] < 0 || idx[k] >= n)
+            return fail(CAPSP_ERR_INVALID, "index %d of entry %d is outside [0, %d)", idx[k], k, n);
+        ++tptr[(size_t)idx[k] + 1];
+    }
+    for (int j = 0; j < n; ++j)
+        tptr[(size_t)j + 1] += tptr[(size_t)j];
+    std::vector<int> fill(tptr.begin(), tptr.end() - 1);
+    for (int i = 0; i < n; ++i)
+        for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+            const int p = fill[(size_t)idx[k]]++;
+            tidx[(size_t)p] = i;
+            src[(size_t)p] = k;
+        }
+    return CAPSP_OK;
+}
+
+// Build the level schedule of view v (host work O(nnz) plus one upload);
+// synchronous.
+static capsp_status_t build_view(capsp_handle_t h, int v)
+{
+    RowView &rv = h->view[v];
+    if (rv.built)
         return CAPSP_OK;
     h->graphs.invalidate();
     const int n = h->n, nnz = h->nnz;
-    const int upper = row_view_upper(h);
+    int upper = row_view_upper(h);
     std::vector<int> idx((size_t)nnz);
     CAPSP_CUDA(cudaMemcpy(idx.data(), h->d_idx, sizeof(int) * (size_t)nnz, cudaMemcpyDeviceToHost));
+    const int *vptr = h->h_ptr.data(), *vidx = idx.data();
+    std::vector<int> tptr, tidx, tsrc;
+    if (v == 1) {
+        CAPSP_TRY(transpose_structure(n, nnz, vptr, vidx, tptr, tidx, tsrc));
+        vptr = tptr.data();
+        vidx = tidx.data();
+        upper = !upper;
+    }
     std::vector<int> order((size_t)n), position((size_t)n), lptr((size_t)n + 1), dsrc((size_t)n);
     const size_t ndeps = (size_t)nnz - (size_t)n;
     std::vector<int> lidx(ndeps > 0 ? ndeps : 1), lsrc(ndeps > 0 ? ndeps : 1);
-    const int levels = capsp_level_schedule(n, h->h_ptr.data(), idx.data(), upper, order.data(),
-                                            position.data(), nullptr);
+    const int levels = capsp_level_schedule(n, vptr, vidx, upper, order.data(), position.data(), nullptr);
     if (levels < 0)
         return fail(CAPSP_ERR_OOM, "host allocation failed while building the level schedule");
-    if (capsp_level_layout(n, h->h_ptr.data(), idx.data(), upper, order.data(), position.data(),
-                           lptr.data(), lidx.data(), lsrc.data(), dsrc.data()) != 0)
+    if (capsp_level_layout(n, vptr, vidx, upper, order.data(), position.data(), lptr.data(), lidx.data(),
+                           lsrc.data(), dsrc.data()) != 0)
         return fail(CAPSP_ERR_INVALID, "misplaced diagonal while building the level schedule");
+    if (v == 1) {
+        for (size_t e = 0; e < ndeps; ++e)
+            lsrc[e] = tsrc[(size_t)lsrc[e]];
+        for (int q = 0; q < n; ++q)
+            dsrc[(size_t)q] = tsrc[(size_t)dsrc[(size_t)q]];
+    }
     const size_t vb = h->vbytes;
-    CAPSP_CUDA(cudaMalloc(&h->d_perm, sizeof(int) * (size_t)n));
-    CAPSP_CUDA(cudaMalloc(&h->d_lptr, sizeof(int) * ((size_t)n + 1)));
+    for (int **p : {&rv.d_perm, &rv.d_lptr, &rv.d_lidx, &rv.d_lsrc, &rv.d_dsrc}) {  // an earlier failed build
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    for (void **p : {&rv.d_lval, &rv.d_linv}) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    CAPSP_CUDA(cudaMalloc(&rv.d_perm, sizeof(int) * (size_t)n));
+    CAPSP_CUDA(cudaMalloc(&rv.d_lptr, sizeof(int) * ((size_t)n + 1)));
     // 4 entries of padding: the row kernels stage a chunk's entries in 16-byte
     // pieces from a 16-byte boundary, up to 3 entries past its last one
-    CAPSP_CUDA(cudaMalloc(&h->d_lidx, sizeof(int) * (lidx.size() + 4)));
-    CAPSP_CUDA(cudaMalloc(&h->d_lsrc, sizeof(int) * lsrc.size()));
-    CAPSP_CUDA(cudaMalloc(&h->d_dsrc, sizeof(int) * (size_t)n));
-    CAPSP_CUDA(cudaMalloc(&h->d_lval, vb * (lidx.size() + 4)));
-    CAPSP_CUDA(cudaMemset(h->d_lidx + lidx.size(), 0, sizeof(int) * 4));
-    CAPSP_CUDA(cudaMemset((char *)h->d_lval + vb * lidx.size(), 0, vb * 4));
-    CAPSP_CUDA(cudaMalloc(&h->d_linv, vb * (size_t)n));
-    CAPSP_CUDA(cudaMemcpy(h->d_perm, order.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
-    CAPSP_CUDA(cudaMemcpy(h->d_lptr, lptr.data(), sizeof(int) * ((size_t)n + 1), cudaMemcpyHostToDevice));
-    CAPSP_CUDA(cudaMemcpy(h->d_lidx, lidx.data(), sizeof(int) * lidx.size(), cudaMemcpyHostToDevice));
-    CAPSP_CUDA(cudaMemcpy(h->d_lsrc, lsrc.data(), sizeof(int) * lsrc.size(), cudaMemcpyHostToDevice));
-    CAPSP_CUDA(cudaMemcpy(h->d_dsrc, dsrc.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
-    h->h_lcum.resize((size_t)n + 1);
+    CAPSP_CUDA(cudaMalloc(&rv.d_lidx, sizeof(int) * (lidx.size() + 4)));
+    CAPSP_CUDA(cudaMalloc(&rv.d_lsrc, sizeof(int) * lsrc.size()));
+    CAPSP_CUDA(cudaMalloc(&rv.d_dsrc, sizeof(int) * (size_t)n));
+    CAPSP_CUDA(cudaMalloc(&rv.d_lval, vb * (lidx.size() + 4)));
+    CAPSP_CUDA(cudaMemset(rv.d_lidx + lidx.size(), 0, sizeof(int) * 4));
+    CAPSP_CUDA(cudaMemset((char *)rv.d_lval + vb * lidx.size(), 0, vb * 4));
+    CAPSP_CUDA(cudaMalloc(&rv.d_linv, vb * (size_t)n));
+    CAPSP_CUDA(cudaMemcpy(rv.d_perm, order.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
+    CAPSP_CUDA(cudaMemcpy(rv.d_lptr, lptr.data(), sizeof(int) * ((size_t)n + 1), cudaMemcpyHostToDevice));
+    CAPSP_CUDA(cudaMemcpy(rv.d_lidx, lidx.data(), sizeof(int) * lidx.size(), cudaMemcpyHostToDevice));
+    CAPSP_CUDA(cudaMemcpy(rv.d_lsrc, lsrc.data(), sizeof(int) * lsrc.size(), cudaMemcpyHostToDevice));
+    CAPSP_CUDA(cudaMemcpy(rv.d_dsrc, dsrc.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
+    rv.h_lcum.resize((size_t)n + 1);
     for (int k = 0; k <= n; ++k)
-        h->h_lcum[k] = lptr[k] + k;
-    h->levels = levels;
-    h->narrow_levels = (long long)n < 4096LL * (long long)levels;
-    h->level_built = true;
+        rv.h_lcum[k] = lptr[k] + k;
+    rv.upper = upper;
+    rv.levels = levels;
+    // levels narrower than ~4k rows: two resident warps per SM for the row
+    // path by default (more rows in flight than a few levels only add pollers)
+    rv.narrow = (long long)n < 4096LL * (long long)levels;
+    rv.built = true;
     int *d_bad = nullptr;
     CAPSP_CUDA(cudaMalloc(&d_bad, sizeof(int)));
     const int big = INT_MAX;
     int bad = INT_MAX;
     cudaError_t e = cudaMemcpy(d_bad, &big, sizeof(int), cudaMemcpyHostToDevice);
-    capsp_status_t s = e == cudaSuccess ? launch_level_refresh(h, d_bad, 0) : CAPSP_ERR_CUDA;
+    capsp_status_t s = e == cudaSuccess ? launch_view_refresh(h, rv, d_bad, 0) : CAPSP_ERR_CUDA;
     if (s == CAPSP_OK)
         e = cudaMemcpy(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost);
     cudaFree(d_bad);
@@ -423,8 +506,8 @@ extern "C" capsp_status_t capsp_analyse(int n, int nnz, const int *ptr, const in
     }
     h->d_err = reinterpret_cast<int *>(h->d_ticket + 64);
     st = refresh_inv_diag(h);
-    if (st == CAPSP_OK && format == CAPSP_FMT_CSR)
-        st = build_level(h);  // the default schedule of the forward solve
+    if (st == CAPSP_OK)
+        st = build_view(h, view_of(h, kOpSolve));  // the default path of the plain solve
     if (st != CAPSP_OK) {
         free_handle(h);
         return st;
@@ -486,10 +569,8 @@ extern "C" capsp_status_t capsp_set_values(capsp_handle_t h, const void *val)
         CAPSP_CUDA(cudaMemcpy(h->d_val, val, h->vbytes * (size_t)h->nnz, cudaMemcpyHostToDevice));
     }
     CAPSP_TRY(refresh_inv_diag(h));
-    if (h->level_built) {
-        CAPSP_TRY(launch_level_refresh(h, h->d_err + 3, 0));
-        CAPSP_CUDA(cudaDeviceSynchronize());
-    }
+    CAPSP_TRY(launch_level_refresh(h, h->d_err + 3, 0));
+    CAPSP_CUDA(cudaDeviceSynchronize());
     return CAPSP_OK;
 }
 
@@ -528,7 +609,7 @@ extern "C" capsp_status_t capsp_set_schedule(capsp_handle_t h, int schedule)
     h->tuned.clear();
     h->graphs.invalidate();
     if (schedule == CAPSP_SCHED_LEVEL)
-        return build_level(h);
+        return build_view(h, 0);
     return CAPSP_OK;
 }
 
@@ -575,10 +656,6 @@ extern "C" capsp_status_t capsp_set_algorithm(capsp_handle_t h, int algorithm)
         return fail(CAPSP_ERR_INVALID, "handle is NULL");
     if (algorithm < CAPSP_ALG_AUTO || algorithm > CAPSP_ALG_SYNCFREE_CSC)
         return fail(CAPSP_ERR_INVALID, "unknown algorithm %d", algorithm);
-    if (algorithm == CAPSP_ALG_SYNCFREE_CSC && h->format != CAPSP_FMT_CSC)
-        return fail(CAPSP_ERR_UNSUPPORTED,
-                    "the warp-per-column kernel solves CSC handles; build the CSC with "
-                    "matrix_transposition and analyse it with CAPSP_FMT_CSC");
     std::lock_guard<std::recursive_mutex> lk(h->mu);
     h->alg = algorithm;
     h->tuned.clear();
@@ -650,19 +727,19 @@ extern "C" capsp_status_t capsp_debug_set_stuck_row(capsp_handle_t h, int row, u
 // rows per mix group for a launch with nrhs right-hand sides
 static int group_rows_for(int nrhs) { return 32 / lanes_for_rhs(nrhs < 32 ? nrhs : 32); }
 
-// Selector table over `group_rows` consecutive schedule positions; its row
-// counts come from the level layout (dependencies + diagonal per position) or,
-// for the natural schedule, from the row pointer of the row-driven view.
-static capsp_status_t ensure_mix(capsp_handle_t h, int group_rows, int border, MixTable **out)
+// Selector table over `group_rows` consecutive schedule positions of view v;
+// its row counts come from the view's level layout (dependencies + diagonal
+// per position) or, for view 0's natural schedule, from the stored row pointer.
+static capsp_status_t ensure_mix(capsp_handle_t h, int v, int group_rows, int border, MixTable **out)
 {
-    const bool level = h->sched == CAPSP_SCHED_LEVEL;
-    MixTable &mt = h->mix[group_rows * 2 + (level ? 1 : 0)];
+    const bool level = view_level(h, v);
+    MixTable &mt = h->mix[(group_rows * 2 + (level ? 1 : 0)) * 2 + v];
     if (mt.d == nullptr || mt.border != border) {
         h->graphs.invalidate();  // a captured launch holds the old table's length
         std::vector<int> table((size_t)h->n + 2);
         double wo = 0.0, eo = 0.0;
-        const int len = level ? capsp_mix_table(h->n, h->h_lcum.data(), 0, group_rows, border, table.data(),
-                                                &wo, &eo)
+        const int len = level ? capsp_mix_table(h->n, h->view[v].h_lcum.data(), 0, group_rows, border,
+                                                table.data(), &wo, &eo)
                               : capsp_mix_table(h->n, h->h_ptr.data(), row_view_upper(h), group_rows, border,
                                                 table.data(), &wo, &eo);
         if (mt.d == nullptr)
@@ -770,23 +847,26 @@ static capsp_status_t ensure_column_order(capsp_handle_t h, int backward)
 // (*cap), whatever the shape.
 // Levels of 32k rows and more on average keep the GPU busy without waiting on
 // the dependency chain: the solve is then bound by throughput, not latency.
-static bool wide_levels(capsp_handle_t h)
+static bool wide_levels(capsp_handle_t h, int v)
 {
-    return h->level_built && (long long)h->n >= 32768LL * (long long)h->levels;
+    const RowView &rv = h->view[v];
+    return rv.built && (long long)h->n >= 32768LL * (long long)rv.levels;
 }
 
-static void row_shape(capsp_handle_t h, const Tuning &tn, int nrhs, int *block, int *bps, bool *cap = nullptr)
+static void row_shape(capsp_handle_t h, int v, const Tuning &tn, int nrhs, int *block, int *bps,
+                      bool *cap = nullptr)
 {
     const int g = lanes_for_rhs(nrhs);
-    const bool narrow = h->narrow_levels && h->sched == CAPSP_SCHED_LEVEL;
+    const bool level = view_level(h, v);
+    const bool narrow = h->view[v].narrow && level;
     if (cap)
-        *cap = g >= 4 && !narrow && h->sched == CAPSP_SCHED_LEVEL;
+        *cap = g >= 4 && !narrow && level;
     *block = tn.block;
     *bps = tn.bps;
     if (!tn.dflt)
         return;
     if (g == 1) {
-        *block = narrow ? 64 : (wide_levels(h) ? 512 : 384);
+        *block = narrow ? 64 : (wide_levels(h, v) ? 512 : 384);
         *bps = 1;
     } else if (g == 2) {
         *block = 256;
@@ -797,11 +877,17 @@ static void row_shape(capsp_handle_t h, const Tuning &tn, int nrhs, int *block, 
     }
 }
 
-static Tuning current_tuning(capsp_handle_t h, int nrhs)
+// launch tuning of an operation with nrhs right-hand sides (autotuned choices
+// cover the plain solve)
+static Tuning current_tuning(capsp_handle_t h, Op op, int nrhs)
 {
-    auto it = h->tuned.find(nrhs);
-    if (it != h->tuned.end())
-        return it->second;
+    if (op == kOpSolve) {
+        auto it = h->tuned.find(nrhs);
+        if (it != h->tuned.end())
+            return it->second;
+    }
+    const int v = view_of(h, op);
+    const RowView &rv = h->view[v];
     Tuning t = h->tune;
     t.border = h->border;
     t.dflt = !h->tune_explicit;
@@ -813,8 +899,8 @@ static Tuning current_tuning(capsp_handle_t h, int nrhs)
     // lane (measured on GB300: 2,048 banded systems with 4-13 entries per row,
     // mixed at the reference's border of 10: 2.98 ms; one lane per row:
     // 1.96 ms).
-    if (h->alg == CAPSP_ALG_AUTO && !h->border_explicit) {
-        if (h->level_built && h->sched == CAPSP_SCHED_LEVEL && (long long)h->n < 32LL * (long long)h->levels)
+    if ((h->alg == CAPSP_ALG_AUTO || h->alg == CAPSP_ALG_SYNCFREE_CSC) && !h->border_explicit) {
+        if (rv.built && view_level(h, v) && (long long)h->n < 32LL * (long long)rv.levels)
             t.border = 1;
         else if (t.border < 32)
             t.border = 32;
@@ -847,14 +933,15 @@ static capsp_status_t ensure_xp(capsp_handle_t h, int nrhs)
     return CAPSP_OK;
 }
 
+// row-driven solve over view v
 template <typename T>
-static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs, int64_t ld,
+static capsp_status_t enqueue_rows(capsp_handle_t h, int v, const T *b, T *x, int nrhs, int64_t ld,
                                    const Tuning &tn, cudaStream_t st)
 {
-    const int view_upper = row_view_upper(h);
-    const bool level = h->sched == CAPSP_SCHED_LEVEL;
+    const bool level = view_level(h, v);
+    const RowView &rv = h->view[v];
     if (level) {
-        CAPSP_TRY(build_level(h));
+        CAPSP_TRY(build_view(h, v));
         CAPSP_TRY(ensure_xp(h, nrhs));
     }
     for (int r0 = 0; r0 < nrhs; r0 += 32) {
@@ -867,7 +954,7 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs,
         if (kind < 0 && lanes_for_rhs(nb) >= 8)
             kind = kRowWrtFst;
         if (kind == kRowMix || kind < 0) {
-            CAPSP_TRY(ensure_mix(h, group_rows_for(nb), tn.border, &mt));
+            CAPSP_TRY(ensure_mix(h, v, group_rows_for(nb), tn.border, &mt));
             if (kind < 0)
                 kind = mt->wo > 0.0 ? kRowMix : kRowWrtFst;
         }
@@ -884,11 +971,11 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs,
         a.idx = h->d_idx;
         a.val = (const T *)h->d_val;
         a.inv_diag = (const T *)h->d_inv;
-        a.perm = level ? h->d_perm : nullptr;
-        a.lptr = h->d_lptr;
-        a.lidx = h->d_lidx;
-        a.lval = (const T *)h->d_lval;
-        a.linv = (const T *)h->d_linv;
+        a.perm = level ? rv.d_perm : nullptr;
+        a.lptr = rv.d_lptr;
+        a.lidx = rv.d_lidx;
+        a.lval = (const T *)rv.d_lval;
+        a.linv = (const T *)rv.d_linv;
         a.xp = (T *)h->d_xp;
         a.ldp = nb;
         a.b = b + r0;
@@ -896,7 +983,7 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs,
         a.ld = ld;
         a.n = h->n;
         a.nrhs = nb;
-        a.upper = view_upper;
+        a.upper = row_view_upper(h);  // read by view 0's natural schedule only
         a.table = kind == kRowMix ? mt->d : nullptr;
         a.table_len = kind == kRowMix ? mt->len : 0;
         a.ticket = h->d_ticket;
@@ -920,7 +1007,7 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs,
             CAPSP_CUDA(cudaEventRecord(h->ev_k0, st));
         int blk = 0, bps = 0;
         bool cap = false;
-        row_shape(h, tn, nb, &blk, &bps, &cap);
+        row_shape(h, v, tn, nb, &blk, &bps, &cap);
         // One lane per row stages each sub-chunk's entries in shared memory
         // with coalesced copies, which shortens the dependency hops of
         // latency-bound FP64 solves (measured on GB300: wide_4m 0.792 -> 0.771
@@ -928,7 +1015,7 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, const T *b, T *x, int nrhs,
         // (2,048 systems with 93k rows per level: 1.66 -> 2.34 ms).  FP32
         // entries are 8 bytes, and there it was mixed (wide_4m 0.715 -> 0.730
         // ms, grad_1m 1.242 -> 1.230 ms), so FP32 walks the rows directly.
-        const bool stage = level && nb == 1 && !wide_levels(h) && sizeof(T) == 8;
+        const bool stage = level && nb == 1 && !wide_levels(h, v) && sizeof(T) == 8;
         CAPSP_CUDA(launch_row_solve<T>(a, kind, tn.R, blk, bps, h->num_sms, cap, stage, st));
         if (prof)
             CAPSP_CUDA(cudaEventRecord(h->ev_k1, st));
@@ -999,21 +1086,36 @@ static capsp_status_t enqueue_cols(capsp_handle_t h, const T *b, T *x, int nrhs,
     return CAPSP_OK;
 }
 
-enum Op { kOpSolve, kOpTranspose, kOpTransposeGrad };
+// grad[k] = -sum_r y[row(k), r] * x[col(k), r] over the stored entries, in
+// chunks of 32 right-hand sides (a CSC handle stores (col, row idx[k]), so y
+// and x swap roles); the first chunk overwrites grad, later ones subtract
+template <typename T>
+static capsp_status_t enqueue_grad(capsp_handle_t h, const T *y, const T *x, T *grad, int nrhs, int64_t ld,
+                                   cudaStream_t st)
+{
+    const bool csr = h->format == CAPSP_FMT_CSR;
+    for (int r0 = 0; r0 < nrhs; r0 += 32) {
+        const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
+        CAPSP_CUDA(launch_grad_val<T>(h->d_ptr, h->d_idx, csr ? y + r0 : x + r0, csr ? x + r0 : y + r0, grad, h->n,
+                                      nb, ld, r0 > 0, st));
+    }
+    return CAPSP_OK;
+}
 
 template <typename T>
 static capsp_status_t enqueue_op(capsp_handle_t h, Op op, const T *in, T *out, const T *xf, T *grad,
                                  int nrhs, int64_t ld, const Tuning &tn, cudaStream_t st)
 {
-    const bool transpose = op != kOpSolve;
-    const bool row_path = (h->format == CAPSP_FMT_CSR) != transpose;
-    if (op == kOpTransposeGrad && h->format != CAPSP_FMT_CSR)
-        return fail(CAPSP_ERR_UNSUPPORTED, "the fused transpose+gradient sweep needs a CSR handle");
-    if (row_path)
-        return enqueue_rows<T>(h, in, out, nrhs, ld, tn, st);
-    // column path: CSC solve (forward for lower) or CSR transpose (backward for lower)
-    const int backward = transpose ? (h->uplo == CAPSP_LOWER) : (h->uplo == CAPSP_UPPER);
-    return enqueue_cols<T>(h, in, out, nrhs, ld, backward, xf, grad, tn, st);
+    if (column_driven(h, op)) {
+        // CSC solve (forward for lower) or CSR transpose (backward for lower),
+        // with the gradient fused into the CSR transpose
+        const int backward = op != kOpSolve ? (h->uplo == CAPSP_LOWER) : (h->uplo == CAPSP_UPPER);
+        return enqueue_cols<T>(h, in, out, nrhs, ld, backward, xf, grad, tn, st);
+    }
+    CAPSP_TRY(enqueue_rows<T>(h, view_of(h, op), in, out, nrhs, ld, tn, st));
+    if (op == kOpTransposeGrad)
+        CAPSP_TRY(enqueue_grad<T>(h, out, xf, grad, nrhs, ld, st));
+    return CAPSP_OK;
 }
 
 static capsp_status_t check_vec_args(capsp_handle_t h, const void *a, const void *b, int nrhs, int64_t ld)
@@ -1032,7 +1134,7 @@ static capsp_status_t check_vec_args(capsp_handle_t h, const void *a, const void
 static capsp_status_t dispatch(capsp_handle_t h, Op op, const void *in, void *out, const void *xf,
                                void *grad, int nrhs, int64_t ld, cudaStream_t st)
 {
-    const Tuning tn = current_tuning(h, nrhs);
+    const Tuning tn = current_tuning(h, op, nrhs);
     if (h->dtype == CAPSP_R_64F)
         return enqueue_op<double>(h, op, (const double *)in, (double *)out, (const double *)xf,
                                   (double *)grad, nrhs, ld, tn, st);
@@ -1079,46 +1181,33 @@ extern "C" capsp_status_t capsp_grad_val(capsp_handle_t h, const void *y, const 
     std::lock_guard<std::recursive_mutex> lk(h->mu);
     DeviceGuard g(h->device);
     cudaStream_t st = (cudaStream_t)stream;
-    // CSR: grad[k] = -y[row] x[col]; CSC stores (col j, row idx[k]): swap roles
-    const bool csr = h->format == CAPSP_FMT_CSR;
-    for (int r0 = 0; r0 < nrhs; r0 += 32) {
-        const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
-        if (h->dtype == CAPSP_R_64F) {
-            const double *yy = (const double *)y + r0, *xx = (const double *)x + r0;
-            CAPSP_CUDA(launch_grad_val<double>(h->d_ptr, h->d_idx, csr ? yy : xx, csr ? xx : yy,
-                                               (double *)grad_val, h->n, nb, ld, r0 > 0, st));
-        } else {
-            const float *yy = (const float *)y + r0, *xx = (const float *)x + r0;
-            CAPSP_CUDA(launch_grad_val<float>(h->d_ptr, h->d_idx, csr ? yy : xx, csr ? xx : yy,
-                                              (float *)grad_val, h->n, nb, ld, r0 > 0, st));
+    if (h->dtype == CAPSP_R_64F)
+        return enqueue_grad<double>(h, (const double *)y, (const double *)x, (double *)grad_val, nrhs, ld, st);
+    return enqueue_grad<float>(h, (const float *)y, (const float *)x, (float *)grad_val, nrhs, ld, st);
+}
+
+// allocate every lazily-built product an operation with nrhs right-hand sides needs
+static capsp_status_t prepare(capsp_handle_t h, int nrhs, Op op)
+{
+    if (column_driven(h, op)) {
+        const int backward = op != kOpSolve ? (h->uplo == CAPSP_LOWER) : (h->uplo == CAPSP_UPPER);
+        CAPSP_TRY(ensure_column_order(h, backward));
+        return ensure_column_scratch(h, nrhs);
+    }
+    const int v = view_of(h, op);
+    if (view_level(h, v)) {
+        CAPSP_TRY(build_view(h, v));
+        CAPSP_TRY(ensure_xp(h, nrhs));
+    }
+    const Tuning tn = current_tuning(h, op, nrhs);
+    if (tn.kind == kRowMix || tn.kind < 0) {
+        MixTable *mt = nullptr;
+        for (int r0 = 0; r0 < nrhs; r0 += 32) {
+            const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
+            CAPSP_TRY(ensure_mix(h, v, group_rows_for(nb), tn.border, &mt));
         }
     }
     return CAPSP_OK;
-}
-
-// allocate every lazily-built product a solve with nrhs right-hand sides needs
-static capsp_status_t prepare(capsp_handle_t h, int nrhs, bool transpose)
-{
-    const bool row_path = (h->format == CAPSP_FMT_CSR) != transpose;
-    if (row_path) {
-        if (h->sched == CAPSP_SCHED_LEVEL) {
-            CAPSP_TRY(build_level(h));
-            CAPSP_TRY(ensure_xp(h, nrhs));
-        }
-        const Tuning tn = current_tuning(h, nrhs);
-        if (tn.kind == kRowMix || tn.kind < 0) {
-            MixTable *mt = nullptr;
-            for (int r0 = 0; r0 < nrhs; r0 += 32) {
-                const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
-                CAPSP_TRY(ensure_mix(h, group_rows_for(nb), tn.border, &mt));
-            }
-        }
-        return CAPSP_OK;
-    }
-    // column path: CSC solve (forward for lower) or CSR transpose (backward for lower)
-    const int backward = transpose ? (h->uplo == CAPSP_LOWER) : (h->uplo == CAPSP_UPPER);
-    CAPSP_TRY(ensure_column_order(h, backward));
-    return ensure_column_scratch(h, nrhs);
 }
 
 extern "C" capsp_status_t capsp_reserve(capsp_handle_t h, int max_nrhs)
@@ -1127,8 +1216,8 @@ extern "C" capsp_status_t capsp_reserve(capsp_handle_t h, int max_nrhs)
         return fail(CAPSP_ERR_INVALID, "need a handle and max_nrhs >= 1");
     std::lock_guard<std::recursive_mutex> lk(h->mu);
     DeviceGuard g(h->device);
-    CAPSP_TRY(prepare(h, max_nrhs, false));
-    CAPSP_TRY(prepare(h, max_nrhs, true));
+    CAPSP_TRY(prepare(h, max_nrhs, kOpSolve));
+    CAPSP_TRY(prepare(h, max_nrhs, kOpTranspose));
     return CAPSP_OK;
 }
 
@@ -1192,8 +1281,8 @@ extern "C" capsp_status_t capsp_solve_host(capsp_handle_t h, const void *b_host,
     // per scattered read over the link, costs more than the copy (2,048
     // systems with 93k rows per level: 5.66 ms in place, 4.80 ms copied; with
     // 4 right-hand sides, 32 bytes per read, 8.97 ms in place, 11.2 copied).
-    void *b_in_place = (h->format == CAPSP_FMT_CSR && h->sched == CAPSP_SCHED_LEVEL &&
-                        !(wide_levels(h) && nrhs == 1))
+    const int v = view_of(h, kOpSolve);
+    void *b_in_place = (!column_driven(h, kOpSolve) && view_level(h, v) && !(wide_levels(h, v) && nrhs == 1))
                            ? pinned_alias(b_host, h->device)
                            : nullptr;
     if (b_in_place) {
@@ -1218,12 +1307,15 @@ extern "C" capsp_status_t capsp_autotune(capsp_handle_t h, const void *b, void *
     DeviceGuard g(h->device);
     cudaStream_t st = (cudaStream_t)stream;
     std::vector<Tuning> cands;
-    const bool row_path = h->format == CAPSP_FMT_CSR;
+    const bool row_path = !column_driven(h, kOpSolve);
+    const int v = view_of(h, kOpSolve);
     const int blocks[3] = {64, 128, 256};
     if (row_path) {
         const int rs[2] = {1, 2};
-        const bool allow_thread = h->alg == CAPSP_ALG_AUTO || h->alg == CAPSP_ALG_WRTFST;
-        const bool allow_mix = h->alg == CAPSP_ALG_AUTO || h->alg == CAPSP_ALG_MIX;
+        // the row path of a CAPSP_ALG_SYNCFREE_CSC handle chooses as AUTO does
+        const int alg = h->alg == CAPSP_ALG_SYNCFREE_CSC ? CAPSP_ALG_AUTO : h->alg;
+        const bool allow_thread = alg == CAPSP_ALG_AUTO || alg == CAPSP_ALG_WRTFST;
+        const bool allow_mix = alg == CAPSP_ALG_AUTO || alg == CAPSP_ALG_MIX;
         const int bpss[3] = {1, 2, 0};
         if (allow_thread) {
             // the default launch shape first: the search never ends worse
@@ -1263,7 +1355,7 @@ extern "C" capsp_status_t capsp_autotune(capsp_handle_t h, const void *b, void *
             MixTable *mt = nullptr;
             for (int r0 = 0; r0 < nrhs && st_all == CAPSP_OK; r0 += 32) {
                 const int nb = nrhs - r0 < 32 ? nrhs - r0 : 32;
-                st_all = ensure_mix(h, group_rows_for(nb), tn.border, &mt);
+                st_all = ensure_mix(h, v, group_rows_for(nb), tn.border, &mt);
             }
         }
         if (st_all != CAPSP_OK)
@@ -1322,8 +1414,8 @@ extern "C" capsp_status_t capsp_graph_solve(capsp_handle_t h, const void *b, voi
     cudaStream_t st = (cudaStream_t)stream;
     // scratch first: a reallocation here invalidates the cache, so the key
     // below carries the generation the capture will be valid for
-    CAPSP_TRY(prepare(h, nrhs, false));
-    const Tuning tn = current_tuning(h, nrhs);
+    CAPSP_TRY(prepare(h, nrhs, kOpSolve));
+    const Tuning tn = current_tuning(h, kOpSolve, nrhs);
     const GraphKey key = {b, x, nrhs, ld, stream, tn.kind, tn.R, tn.block, tn.bps, tn.border, tn.dflt ? 1 : 0,
                           h->graphs.generation()};
     cudaGraphExec_t *exec_p = h->graphs.find(key);
@@ -1412,21 +1504,22 @@ extern "C" capsp_status_t capsp_get_info(capsp_handle_t h, capsp_info_t *info)
     info->uplo = h->uplo;
     info->analyse_ms = h->analyse_ms;
     info->num_sms = h->num_sms;
-    Tuning tn = current_tuning(h, 1);
+    Tuning tn = current_tuning(h, kOpSolve, 1);
     info->rows_per_thread = tn.R;
     int blk = tn.block, bps = tn.bps;
-    if (h->format == CAPSP_FMT_CSR)
-        row_shape(h, tn, 1, &blk, &bps);
+    const int v = view_of(h, kOpSolve);
+    if (!column_driven(h, kOpSolve))
+        row_shape(h, v, tn, 1, &blk, &bps);
     info->block_threads = blk;
     info->blocks_per_sm = bps;
-    info->schedule = h->sched;
-    info->levels = h->levels;
+    info->schedule = view_level(h, v) ? CAPSP_SCHED_LEVEL : CAPSP_SCHED_NATURAL;
+    info->levels = h->view[v].levels;
     info->cached_graphs = (int)h->graphs.size();
-    if (h->format == CAPSP_FMT_CSC) {
+    if (column_driven(h, kOpSolve)) {
         info->algorithm = CAPSP_ALG_SYNCFREE_CSC;
     } else {
-        int alg = h->alg;
-        auto mit = h->mix.find(32 * 2 + (h->sched == CAPSP_SCHED_LEVEL ? 1 : 0));
+        int alg = h->alg == CAPSP_ALG_SYNCFREE_CSC ? CAPSP_ALG_AUTO : h->alg;
+        auto mit = h->mix.find((32 * 2 + (view_level(h, v) ? 1 : 0)) * 2 + v);
         if (mit != h->mix.end() && mit->second.d) {
             info->mix_len = mit->second.len;
             info->warp_occupy = mit->second.wo;

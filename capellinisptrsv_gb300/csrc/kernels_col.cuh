@@ -378,54 +378,110 @@ cudaError_t launch_inv_diag(const int *ptr, const T *val, T *inv, int n, int dia
     return cudaGetLastError();
 }
 
-// warp per row: 32/G entries x G right-hand sides per pass
-template <typename T, int G>
-__global__ void grad_val_kernel(const int *__restrict__ rowptr, const int *__restrict__ colidx,
-                                const T *__restrict__ y, const T *__restrict__ x,
-                                T *__restrict__ grad, int n, int nrhs, long long ld,
-                                int accumulate)
+// 16-byte vector of T (the rows of own/other are read in these when every
+// row starts on a 16-byte boundary)
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<double> {
+    typedef double2 V;
+    static constexpr int W = 2;
+    static __device__ __forceinline__ void put(V v, double *r)
+    {
+        r[0] = v.x;
+        r[1] = v.y;
+    }
+};
+template <>
+struct Vec16<float> {
+    typedef float4 V;
+    static constexpr int W = 4;
+    static __device__ __forceinline__ void put(V v, float *r)
+    {
+        r[0] = v.x;
+        r[1] = v.y;
+        r[2] = v.z;
+        r[3] = v.w;
+    }
+};
+
+// r[0..NR) = p[0..nrhs), zero beyond nrhs; VEC: nrhs == NR, 16-byte aligned
+template <typename T, int NR, bool VEC>
+__device__ __forceinline__ void load_rhs(const T *__restrict__ p, int nrhs, T (&r)[NR])
 {
-    constexpr int EPW = 32 / G;
-    const int lane = threadIdx.x & 31;
-    const int es = lane / G, g = lane % G;
-    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long i = warp; i < n; i += nwarps) {
-        const int s = rowptr[i], e = rowptr[i + 1];
-        const T yi = g < nrhs ? y[(size_t)i * ld + g] : T(0);
-        for (int kb = s; kb < e; kb += EPW) {
-            const int k = kb + es;
-            T prod = T(0);
-            if (k < e && g < nrhs)
-                prod = yi * x[(size_t)colidx[k] * ld + g];
+    if (VEC) {
+        typedef Vec16<T> VT;
 #pragma unroll
-            for (int off = G / 2; off >= 1; off >>= 1)
-                prod += __shfl_xor_sync(kFullMask, prod, off);
-            if (k < e && g == 0)
-                grad[k] = accumulate ? grad[k] - prod : -prod;
-        }
+        for (int v = 0; v < NR / VT::W; ++v)
+            VT::put(__ldg(reinterpret_cast<const typename VT::V *>(p) + v), r + v * VT::W);
+    } else {
+#pragma unroll
+        for (int q = 0; q < NR; ++q)
+            r[q] = q < nrhs ? __ldg(p + q) : T(0);
     }
 }
 
+// grad[k] = -sum_r own[i, r] * other[idx[k], r] for the entries k of stored
+// row i: one thread per row, own[i, :] in registers and each entry's sum over
+// the right-hand sides one FMA chain inside the thread.  Splitting the
+// right-hand sides over lanes instead costs a shuffle reduction per entry,
+// and its adds run on GB300's narrow FP64 pipe: on grad_1m with 16 RHS that
+// warp-per-row kernel took 1.47 ms.
+template <typename T, int NR, bool VEC>
+__global__ void __launch_bounds__(256) grad_val_kernel(const int *__restrict__ rowptr,
+                                                       const int *__restrict__ colidx,
+                                                       const T *__restrict__ own, const T *__restrict__ other,
+                                                       T *__restrict__ grad, int n, int nrhs, long long ld,
+                                                       int accumulate)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    T yi[NR];
+    load_rhs<T, NR, VEC>(own + (size_t)i * ld, nrhs, yi);
+    const int s = __ldg(rowptr + i), e = __ldg(rowptr + i + 1);
+    for (int k = s; k < e; ++k) {
+        T xr[NR];
+        load_rhs<T, NR, VEC>(other + (size_t)__ldg(colidx + k) * ld, nrhs, xr);
+        T acc = T(0);
+#pragma unroll
+        for (int q = 0; q < NR; ++q)
+            acc = fma(yi[q], xr[q], acc);
+        grad[k] = accumulate ? grad[k] - acc : -acc;
+    }
+}
+
+template <typename T, int NR>
+static cudaError_t launch_grad_nr(const int *rowptr, const int *colidx, const T *own, const T *other, T *grad,
+                                  int n, int nrhs, long long ld, int accumulate, cudaStream_t st)
+{
+    const unsigned blocks = (unsigned)(((long long)n + 255) / 256);
+    const int w = Vec16<T>::W;
+    const bool vec = NR % w == 0 && nrhs == NR && ld % w == 0 && ((uintptr_t)own & 15) == 0 &&
+                     ((uintptr_t)other & 15) == 0;
+    if (vec)
+        grad_val_kernel<T, NR, (NR % Vec16<T>::W == 0)>
+            <<<blocks, 256, 0, st>>>(rowptr, colidx, own, other, grad, n, nrhs, ld, accumulate);
+    else
+        grad_val_kernel<T, NR, false><<<blocks, 256, 0, st>>>(rowptr, colidx, own, other, grad, n, nrhs, ld,
+                                                              accumulate);
+    return cudaGetLastError();
+}
+
+// nrhs <= 32 right-hand sides, rows at stride ld
 template <typename T>
-cudaError_t launch_grad_val(const int *rowptr, const int *colidx, const T *y, const T *x,
+cudaError_t launch_grad_val(const int *rowptr, const int *colidx, const T *own, const T *other,
                             T *grad_val, int n, int nrhs, long long ld, int accumulate,
                             cudaStream_t st)
 {
-    long long blocks = ((long long)n * 32 + 255) / 256;
-    if (blocks > 65536)
-        blocks = 65536;
-    if (blocks < 1)
-        blocks = 1;
     switch (lanes_for_rhs(nrhs)) {
-    case 1: grad_val_kernel<T, 1><<<(unsigned)blocks, 256, 0, st>>>(rowptr, colidx, y, x, grad_val, n, nrhs, ld, accumulate); break;
-    case 2: grad_val_kernel<T, 2><<<(unsigned)blocks, 256, 0, st>>>(rowptr, colidx, y, x, grad_val, n, nrhs, ld, accumulate); break;
-    case 4: grad_val_kernel<T, 4><<<(unsigned)blocks, 256, 0, st>>>(rowptr, colidx, y, x, grad_val, n, nrhs, ld, accumulate); break;
-    case 8: grad_val_kernel<T, 8><<<(unsigned)blocks, 256, 0, st>>>(rowptr, colidx, y, x, grad_val, n, nrhs, ld, accumulate); break;
-    case 16: grad_val_kernel<T, 16><<<(unsigned)blocks, 256, 0, st>>>(rowptr, colidx, y, x, grad_val, n, nrhs, ld, accumulate); break;
-    default: grad_val_kernel<T, 32><<<(unsigned)blocks, 256, 0, st>>>(rowptr, colidx, y, x, grad_val, n, nrhs, ld, accumulate); break;
+    case 1: return launch_grad_nr<T, 1>(rowptr, colidx, own, other, grad_val, n, nrhs, ld, accumulate, st);
+    case 2: return launch_grad_nr<T, 2>(rowptr, colidx, own, other, grad_val, n, nrhs, ld, accumulate, st);
+    case 4: return launch_grad_nr<T, 4>(rowptr, colidx, own, other, grad_val, n, nrhs, ld, accumulate, st);
+    case 8: return launch_grad_nr<T, 8>(rowptr, colidx, own, other, grad_val, n, nrhs, ld, accumulate, st);
+    case 16: return launch_grad_nr<T, 16>(rowptr, colidx, own, other, grad_val, n, nrhs, ld, accumulate, st);
+    default: return launch_grad_nr<T, 32>(rowptr, colidx, own, other, grad_val, n, nrhs, ld, accumulate, st);
     }
-    return cudaGetLastError();
 }
 
 }  // namespace capsp

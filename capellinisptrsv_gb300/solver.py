@@ -332,7 +332,8 @@ class TriangularSolver:
         return x2
 
     def solve_transpose(self, g, y=None, stream=None):
-        """y = A^{-T} g, column-driven on the same arrays (no transpose built)."""
+        """y = A^{-T} g: over the handle's transposed copy, or column-driven on the
+        stored arrays under algorithm "syncfree_csc" (CSR handles)."""
         g, k, ld = self._vec(g, "g")
         y = self._out_like(g, y)
         N.check(N.lib.capsp_solve_transpose(self._h, _ptr(g), _ptr(y), k, ld,
@@ -340,7 +341,8 @@ class TriangularSolver:
         return y
 
     def solve_transpose_grad(self, g, x, y=None, grad_val=None, stream=None):
-        """Fused backward: y = A^{-T} g and grad_val[k] = -sum_r y[row_k, r] x[col_k, r]."""
+        """Backward: y = A^{-T} g and grad_val[k] = -sum_r y[row_k, r] x[col_k, r]
+        (fused into the column-driven sweep under "syncfree_csc")."""
         g, k, ld = self._vec(g, "g")
         x, kx, ldx = self._vec(x, "x")
         if (kx, ldx) != (k, ld):

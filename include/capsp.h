@@ -72,14 +72,20 @@ typedef enum capsp_uplo {
     CAPSP_UPPER = 1    /* CSR: diagonal first in each row; CSC: diagonal last in each column  */
 } capsp_uplo_t;
 
-/* Row-driven solve algorithms (CSR handles).  CSC handles always use the
- * column-driven sync-free kernel. */
+/* Solve algorithms.  A handle solves the orientation it stores (CSR rows, or
+ * the transpose of a CSC matrix) by walking its rows; the other orientation
+ * (the plain solve of a CSC handle, the transpose of a CSR handle) walks the
+ * rows of a transposed copy of the structure that the handle builds once on
+ * the host, whose entries point back into the stored values.  The row-driven
+ * algorithms below apply to both; CAPSP_ALG_SYNCFREE_CSC instead solves the
+ * other orientation column by column on the stored arrays. */
 typedef enum capsp_algorithm {
     CAPSP_ALG_AUTO = 0,        /* mix when the selector finds heavy row groups, else WRTFST */
     CAPSP_ALG_WRTFST = 1,      /* thread per row, write-first (CUDA/ourWrtFst) */
     CAPSP_ALG_TWOPART = 2,     /* thread per row, out-of-warp then in-warp phases (CUDA/our2Part) */
     CAPSP_ALG_MIX = 3,         /* thread or warp per row by nnz/row of 32-row groups (CUDA/mix) */
-    CAPSP_ALG_SYNCFREE_CSC = 4 /* warp per column, atomic partial sums + arrival counts (CUDA/SyncFree_csc) */
+    CAPSP_ALG_SYNCFREE_CSC = 4 /* warp per column, atomic partial sums + arrival counts (CUDA/SyncFree_csc),
+                                  for the orientation a handle does not store; rows as AUTO */
 } capsp_algorithm_t;
 
 /* Order in which the row-driven kernels start rows.  Any order that lists a
@@ -110,7 +116,8 @@ typedef struct capsp_info {
     int dtype;
     int format;
     int uplo;
-    int algorithm;          /* algorithm the next CSR solve will use (AUTO resolved) */
+    int algorithm;          /* algorithm the next plain solve will use (AUTO resolved once
+                               its selector table exists) */
     int mix_len;            /* entries of the mix virtual-warp table (0 until built) */
     double warp_occupy;     /* rows handled warp-per-row / n   (mix/spts_..._wrt.h:152-156) */
     double element_occupy;  /* nnz in warp-per-row rows / nnz */
@@ -119,8 +126,8 @@ typedef struct capsp_info {
     int block_threads;
     int blocks_per_sm;
     int num_sms;
-    int schedule;           /* capsp_schedule_t of the row-driven kernels */
-    int levels;             /* dependency levels (0 until a level schedule was built) */
+    int schedule;           /* capsp_schedule_t of the plain solve's rows */
+    int levels;             /* dependency levels of the plain solve's rows (0 until built) */
     int cached_graphs;      /* instantiated graphs held for capsp_graph_solve; every change that a
                                captured solve depends on (scratch growth, new value pointer,
                                schedule, tuning, wait budget, debug hooks) drops them all */
@@ -136,7 +143,8 @@ const char *capsp_last_error(void);
 /* Analyse an n-by-n triangular matrix.  Checks the structure (diagonal
  * present at the documented end of every row/column, all other indices on the
  * triangular side, nonzero diagonal), uploads host arrays (or borrows device
- * arrays with CAPSP_DEVICE_POINTERS) and precomputes 1/diag.
+ * arrays with CAPSP_DEVICE_POINTERS), precomputes 1/diag and builds the level
+ * schedule of the plain solve (of the transposed structure for CSC).
  * Replaces the upload + analysis half of spts_syncfree_cuda_csr_wrt
  * (CUDA/ourWrtFst/spts_syncfree_cuda_csr_wrt.h:66-124) and the in-degree
  * analyser of sptrsv_syncfree_cuda (CUDA/SyncFree_csc/spts_syncfree_cuda2.h:139-160). */
@@ -178,12 +186,13 @@ capsp_status_t capsp_get_info(capsp_handle_t h, capsp_info_t *info);
  * neither. */
 capsp_status_t capsp_set_l2_policy(capsp_handle_t h, int mode);
 
-/* Choose the row-driven algorithm for CSR handles (capsp_algorithm_t). */
+/* Choose the solve algorithm (capsp_algorithm_t). */
 capsp_status_t capsp_set_algorithm(capsp_handle_t h, int algorithm);
 
-/* Row-driven schedule (capsp_schedule_t).  CAPSP_SCHED_LEVEL builds the level
- * order on first use if capsp_analyse did not (CSC handles build it for their
- * transposed solves); the build is host work proportional to nnz. */
+/* Schedule of the rows of the stored orientation (capsp_schedule_t).
+ * CAPSP_SCHED_LEVEL builds the level order on first use if capsp_analyse did
+ * not; the build is host work proportional to nnz.  The transposed copy is
+ * always level-ordered. */
 capsp_status_t capsp_set_schedule(capsp_handle_t h, int schedule);
 
 /* Mix selector threshold: 32-row groups whose mean nnz/row is >= border go
@@ -214,21 +223,24 @@ capsp_status_t capsp_set_backoff(capsp_handle_t h, unsigned sleep_max_ns);
 capsp_status_t capsp_solve(capsp_handle_t h, const void *b, void *x, int nrhs,
                            int64_t ld, void *stream);
 
-/* Solve A^T Y = G without building A^T: the rows of a CSR matrix are walked
- * as columns of A^T by the column-driven sync-free kernel, the BACKWARD mode of
+/* Solve A^T Y = G.  A CSR handle walks the rows of its transposed copy (built
+ * on first use), or under CAPSP_ALG_SYNCFREE_CSC its own rows as columns of
+ * A^T with the column-driven kernel, the BACKWARD mode of
  * sptrsv_syncfree_cuda_executor_update (CUDA/SyncFree_csc/spts_syncfree_cuda2.h:50-82)
- * and of the serial executor (openCL/SynFree_csc/sptrsv_syncfree_serialref.h:73-102). */
+ * and of the serial executor (openCL/SynFree_csc/sptrsv_syncfree_serialref.h:73-102).
+ * A CSC handle walks its stored columns as rows of A^T. */
 capsp_status_t capsp_solve_transpose(capsp_handle_t h, const void *g, void *y,
                                      int nrhs, int64_t ld, void *stream);
 
 /* grad_val[k] = -sum_r y[row(k), r] * x[col(k), r] over the stored nonzeros
- * (CSR handles).  No reference counterpart: the gradient of L x = b with
+ * (CSR or CSC).  No reference counterpart: the gradient of L x = b with
  * respect to the values of L, given y = L^{-T} g. */
 capsp_status_t capsp_grad_val(capsp_handle_t h, const void *y, const void *x,
                               void *grad_val, int nrhs, int64_t ld, void *stream);
 
-/* Fused backward of x = L^{-1} b: y = L^{-T} g and grad_val from the same
- * column-driven sweep (CSR handles).  No reference counterpart. */
+/* Backward of x = L^{-1} b: y = L^{-T} g (as capsp_solve_transpose), then
+ * grad_val as capsp_grad_val; under CAPSP_ALG_SYNCFREE_CSC a CSR handle fuses
+ * grad_val into its column-driven sweep.  No reference counterpart. */
 capsp_status_t capsp_solve_transpose_grad(capsp_handle_t h, const void *g,
                                           const void *x, void *y, void *grad_val,
                                           int nrhs, int64_t ld, void *stream);

@@ -108,12 +108,14 @@ def test_graph_cache_after_scratch_growth(batch):
     assert s.info()["cached_graphs"] == 0
 
 
-def test_graph_solve_csc_first_call():
-    """A CSC handle's first solve through graph replay: the column visiting
-    order and the scratch are built before the capture starts."""
+@pytest.mark.parametrize("algorithm", ["auto", "syncfree_csc"])
+def test_graph_solve_csc_first_call(algorithm):
+    """A CSC handle's first solve through graph replay: the publication
+    scratch (transposed view) or the column visiting order and the
+    sum-and-count words (column-driven) are built before the capture starts."""
     m = cs.generate("plain_20k", seed=0)
     cp, ri, cv = cs.matrix_transposition(m.n, m.n, m.nnz, m.rowptr, m.colidx, m.val)
-    s = cs.TriangularSolver(t(cp), t(ri), t(cv), fmt="csc")
+    s = cs.TriangularSolver(t(cp), t(ri), t(cv), fmt="csc", algorithm=algorithm)
     b = np.random.default_rng(3).standard_normal(m.n)
     bd, x = t(b), torch.empty(m.n, dtype=torch.float64, device=DEV)
     st = torch.cuda.Stream()

@@ -14,8 +14,9 @@ CUDA/SyncFree_csc/spts_syncfree_cuda2.h:245-264).
     from a CUDA graph as the benchmark runs it; every system is checked at
     k = 1 and 4, every fourth system at k = 16 and 32;
   * grad_1m: n = 1,048,576 with 16 right-hand sides through the autograd
-    function: x, grad_b = L^{-T}(x - x*) and grad_val = -grad_b[row] x[col]
-    against the serial forward, the serial adjoint and the oracle grad_val.
+    function, whose backward runs over the transposed view or column-driven:
+    x, grad_b = L^{-T}(x - x*) and grad_val = -grad_b[row] x[col] against the
+    serial forward, the serial adjoint and the oracle grad_val.
     (The finite-difference check runs at n = 20,000 in test_gpu_autograd.py:
     at 1M rows a central difference with h = 1e-6 is dominated by rounding.)
 
@@ -91,7 +92,10 @@ def test_batched_full_size(full_batch, k, stride):
     assert worst <= TOL64, worst
 
 
-def test_grad_1m_full_size_16rhs():
+@pytest.mark.parametrize("algorithm", ["auto", "syncfree_csc"])
+def test_grad_1m_full_size_16rhs(algorithm):
+    """Backward over the transposed view plus the gradient pass (auto), or the
+    column-driven transpose with the gradient fused (syncfree_csc)."""
     m = cs.generate("grad_1m", seed=0)
     n, k = m.n, 16
     assert n == 1_048_576
@@ -99,7 +103,7 @@ def test_grad_1m_full_size_16rhs():
     xs_h = cs.normal(n * k, seed=0, stream=2).reshape(n, k)
     val = dev(m.val).requires_grad_(True)
     b = dev(b_h).requires_grad_(True)
-    solver = cs.TriangularSolver(dev(m.rowptr), dev(m.colidx), val.detach())
+    solver = cs.TriangularSolver(dev(m.rowptr), dev(m.colidx), val.detach(), algorithm=algorithm)
     x = cs.sptrsv(solver, val, b)
     loss = 0.5 * ((x - dev(xs_h)) ** 2).sum()
     loss.backward()

@@ -110,8 +110,10 @@ EDGE = ["single", "diagonal_only", "bidiagonal_chain", "stride64_chain", "dense_
 
 @pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("name", EDGE)
-@pytest.mark.parametrize("alg", ["wrtfst", "twopart", "mix"])
+@pytest.mark.parametrize("alg", ["wrtfst", "twopart", "mix", "syncfree_csc"])
 def test_edge_cases_against_golden(golden, name, alg, schedule):
+    """Forward and transposed solves; the transposes walk the transposed view
+    with the row kernel of `alg`, or (syncfree_csc) the stored rows as columns."""
     rp, ci, v = (golden[f"edge_{name}_{k}"] for k in ("rowptr", "colidx", "val"))
     n = len(rp) - 1
     b1 = np.random.default_rng(11).standard_normal(n)
@@ -125,16 +127,22 @@ def test_edge_cases_against_golden(golden, name, alg, schedule):
     s.status()
 
 
+TRANSPOSE_PATHS = {"rows": "auto", "columns": "syncfree_csc"}
+
+
+@pytest.mark.parametrize("path", list(TRANSPOSE_PATHS))
 @pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("nrhs", [1, 2, 3, 4, 8, 16, 32, 40])
-def test_multi_rhs_forward_adjoint_grad(nrhs, schedule):
+def test_multi_rhs_forward_adjoint_grad(nrhs, schedule, path):
+    """The transposes run over the transposed view (rows, then the gradient
+    pass) or column-driven over the stored rows with the gradient fused."""
     m = cs.generate(n=30_000, kmin=1, kmax=9, band=3000, seed=nrhs)
     b = np.random.default_rng(nrhs).standard_normal((m.n, nrhs))
     g = np.random.default_rng(nrhs + 100).standard_normal((m.n, nrhs))
     xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
     yo = oracle.solve_csr_transpose(m.rowptr, m.colidx, m.val, g)
     go = oracle.grad_val(m.rowptr, m.colidx, yo, xo)
-    s = solver_for(m, schedule=schedule)
+    s = solver_for(m, schedule=schedule, algorithm=TRANSPOSE_PATHS[path])
     x = s.solve(dev(b))
     y, gv = s.solve_transpose_grad(dev(g), x)
     y2 = s.solve_transpose(dev(g))
@@ -147,9 +155,11 @@ def test_multi_rhs_forward_adjoint_grad(nrhs, schedule):
     assert rel_inf_err(host(gv2), go) <= TOL64
 
 
+@pytest.mark.parametrize("path", list(TRANSPOSE_PATHS))
 @pytest.mark.parametrize("nrhs", [1, 4, 16])
-def test_f32_forward_adjoint_grad(nrhs):
-    """FP32 through the column kernel's 8-byte sum-and-count words, against the FP64 oracle."""
+def test_f32_forward_adjoint_grad(nrhs, path):
+    """FP32 over the transposed view, and through the column kernel's 8-byte
+    sum-and-count words, against the FP64 oracle."""
     m = cs.generate(n=30_000, kmin=1, kmax=9, band=3000, seed=60 + nrhs)
     shape = (m.n, nrhs) if nrhs > 1 else (m.n,)
     b = np.random.default_rng(nrhs).standard_normal(shape)
@@ -157,7 +167,7 @@ def test_f32_forward_adjoint_grad(nrhs):
     xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
     yo = oracle.solve_csr_transpose(m.rowptr, m.colidx, m.val, g)
     go = oracle.grad_val(m.rowptr, m.colidx, yo, xo)
-    s = solver_for(m, np.float32)
+    s = solver_for(m, np.float32, algorithm=TRANSPOSE_PATHS[path])
     x = s.solve(dev(b.astype(np.float32)))
     y, gv = s.solve_transpose_grad(dev(g.astype(np.float32)), x)
     s.status()
@@ -198,6 +208,21 @@ def test_wide_4m_full_size_fp64_and_fp32(schedule):
     x32 = host(s32.solve(dev(b32)))
     assert rel_inf_err(x32, x32o) <= TOL32
     print(f"wide_4m FP32 vs FP64 oracle: {rel_inf_err(x32, xo):.3e}")
+
+
+@pytest.mark.parametrize("path", list(TRANSPOSE_PATHS))
+def test_wide_4m_full_size_csc(path):
+    """The 4M-row workload as a CSC handle (the reference's SyncFree_csc input),
+    solved over the transposed view or column by column, against the oracle."""
+    m = cs.generate("wide_4m", seed=0)
+    _, b = cs.get_x_b(m.n, m.n, m.rowptr, m.colidx, m.val)
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)
+    cp, ri, cv = cs.matrix_transposition(m.n, m.n, m.nnz, m.rowptr, m.colidx, m.val)
+    s = cs.TriangularSolver(dev(cp), dev(ri), dev(cv), fmt="csc", algorithm=TRANSPOSE_PATHS[path])
+    x = host(s.solve(dev(b)))
+    s.status()
+    assert rel_inf_err(x, xo) <= TOL64
+    assert np.max(np.abs(x - 1.0)) <= 1e-4  # the reference's own self-check (x_ref = ones)
 
 
 @pytest.mark.parametrize("schedule", SCHEDULES)
@@ -259,20 +284,24 @@ def test_upper_csr_warp_per_row(schedule, k):
     assert rel_inf_err(y, yo) <= TOL64
 
 
+@pytest.mark.parametrize("path", list(TRANSPOSE_PATHS))
 @pytest.mark.parametrize("schedule", SCHEDULES)
-def test_upper_csr_and_csc_paths(schedule):
-    """Upper-triangular CSR (backward substitution) and the CSC warp-per-column
-    kernel, forward and transposed, against the oracle on the same matrix."""
+def test_upper_csr_and_csc_paths(schedule, path):
+    """Upper-triangular CSR (backward substitution) and CSC handles, forward
+    and transposed, against the oracle on the same matrix.  A CSC solve walks
+    the transposed view (rows) or the stored columns (the warp-per-column
+    kernel); so does the transpose of the upper CSR handle."""
     m = cs.generate(n=20_000, kmin=1, kmax=6, band=900, seed=5)
     cp, ri, cv = cs.matrix_transposition(m.n, m.n, m.nnz, m.rowptr, m.colidx, m.val)
     b = cs.normal(m.n, seed=6)
     xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)   # L x = b
     yo = oracle.solve_csr_transpose(m.rowptr, m.colidx, m.val, b)  # L^T y = b
     # CSC of L == CSR of U = L^T (diagonal first in each row)
-    up = cs.TriangularSolver(dev(cp), dev(ri), dev(cv), uplo="upper", schedule=schedule)
+    alg = TRANSPOSE_PATHS[path]
+    up = cs.TriangularSolver(dev(cp), dev(ri), dev(cv), uplo="upper", schedule=schedule, algorithm=alg)
     assert rel_inf_err(host(up.solve(dev(b))), yo) <= TOL64
     assert rel_inf_err(host(up.solve_transpose(dev(b))), xo) <= TOL64
-    csc = cs.TriangularSolver(dev(cp), dev(ri), dev(cv), fmt="csc", schedule=schedule)
+    csc = cs.TriangularSolver(dev(cp), dev(ri), dev(cv), fmt="csc", schedule=schedule, algorithm=alg)
     assert rel_inf_err(host(csc.solve(dev(b))), xo) <= TOL64
     assert rel_inf_err(host(csc.solve_transpose(dev(b))), yo) <= TOL64
     b4 = np.random.default_rng(4).standard_normal((m.n, 4))
@@ -280,6 +309,7 @@ def test_upper_csr_and_csc_paths(schedule):
                        oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b4)) <= TOL64
     up.status()
     csc.status()
+    assert (csc.info()["algorithm"] == 4) == (path == "columns")
 
 
 def test_set_values_refreshes(plain20k):
