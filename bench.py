@@ -936,9 +936,10 @@ def measure_autograd(args, cpu_seconds):
                                      "(upper CSR) + one grad_val pass"},
            "speedup_vs_loop": loop_ms / ms, "loop_vs_autograd_rel_err": agree, "clocks": clk.summary(),
            "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(2 * n * k * 8), "d2h_bytes_per_step": 8},
-           # forward and backward each: 1/diag + the level values of both
-           # views (3), pending fill, row solve; the backward adds grad_val
-           "gpu_launches_per_step": 11}
+           # forward: 1/diag + the level values of both views (3), pending
+           # fill, row solve; backward: pending fill, row solve over the
+           # transposed view, grad_val (no refresh: the values are still bound)
+           "gpu_launches_per_step": 8}
     out["cpu_baseline"] = None
     if cpu_seconds > 0:
         cpu, (xc, yc, gc) = _cpu_autograd(m, b_h, xs_h, cpu_seconds)

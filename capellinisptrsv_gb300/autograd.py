@@ -32,7 +32,10 @@ class SparseTriangularSolve(torch.autograd.Function):
     def backward(ctx, gx: torch.Tensor):
         val, x = ctx.saved_tensors
         solver: TriangularSolver = ctx.solver
-        solver.refresh_values(val.detach())
+        # the forward's values, unless another forward re-bound the solver
+        # since (autograd rejects a saved tensor modified in place, so the
+        # same tensor at the same version holds the same values)
+        solver.refresh_values_if_rebound(val.detach())
         gx = gx.contiguous()
         need_val, need_b = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
         if need_val:

@@ -264,7 +264,10 @@ static capsp_status_t launch_view_refresh(capsp_handle_t h, const RowView &rv, i
 // ... of every built view
 static capsp_status_t launch_level_refresh(capsp_handle_t h, int *bad, cudaStream_t st)
 {
-    for (const RowView &rv : h->view)
+    // Eager, for every built view: a solve captured in a caller's CUDA graph
+    // replays with whatever values the views hold, so a refresh outside the
+    // graph must not be deferred to a later solve
+    for (RowView &rv : h->view)
         CAPSP_TRY(launch_view_refresh(h, rv, bad, st));
     return CAPSP_OK;
 }

@@ -239,4 +239,20 @@ struct Spin {
     }
 };
 
+// Owner, among a warp's 32-row group, of entry k: the largest lane l < nr whose
+// row start (held in `start` by lane l) is <= k; rows without entries share
+// their successor's start and never own one.  Every lane must call it.
+__device__ __forceinline__ int group_row_of(int start, int k, int nr)
+{
+    int lo = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+        const int cand = lo + step;
+        const int sv = __shfl_sync(kFullMask, start, cand & 31);
+        if (cand < nr && sv <= k)
+            lo = cand;
+    }
+    return lo;
+}
+
 }  // namespace capsp

@@ -421,12 +421,15 @@ __device__ __forceinline__ void load_rhs(const T *__restrict__ p, int nrhs, T (&
     }
 }
 
-// grad[k] = -sum_r own[i, r] * other[idx[k], r] for the entries k of stored
-// row i: one thread per row, own[i, :] in registers and each entry's sum over
-// the right-hand sides one FMA chain inside the thread.  Splitting the
-// right-hand sides over lanes instead costs a shuffle reduction per entry,
-// and its adds run on GB300's narrow FP64 pipe: on grad_1m with 16 RHS that
-// warp-per-row kernel took 1.47 ms.
+// grad[k] = -sum_r own[i, r] * other[idx[k], r] for every stored entry k of
+// row i.  A warp takes 32 consecutive rows and walks their entries one per
+// lane (each lane finds its entry's row among the group's row starts), so
+// every lane does the same work: each entry's sum over the right-hand sides
+// is one FMA chain in its lane, and the FP64 pipe -- the bound on GB300 --
+// issues no instruction for idle lanes.  (One thread per row idles the lanes
+// of short rows while the warp's longest row finishes: grad_1m with 16 RHS
+// 0.357 -> 0.268 ms, wide_4m 1.37 -> 0.743 ms; lanes split by right-hand
+// side add a shuffle reduction per entry: 0.58 ms.)
 template <typename T, int NR, bool VEC>
 __global__ void __launch_bounds__(256) grad_val_kernel(const int *__restrict__ rowptr,
                                                        const int *__restrict__ colidx,
@@ -434,20 +437,27 @@ __global__ void __launch_bounds__(256) grad_val_kernel(const int *__restrict__ r
                                                        T *__restrict__ grad, int n, int nrhs, long long ld,
                                                        int accumulate)
 {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n)
+    const int lane = threadIdx.x & 31;
+    const long long r0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+    if (r0 >= n)
         return;
-    T yi[NR];
-    load_rhs<T, NR, VEC>(own + (size_t)i * ld, nrhs, yi);
-    const int s = __ldg(rowptr + i), e = __ldg(rowptr + i + 1);
-    for (int k = s; k < e; ++k) {
-        T xr[NR];
-        load_rhs<T, NR, VEC>(other + (size_t)__ldg(colidx + k) * ld, nrhs, xr);
-        T acc = T(0);
+    const int nr = (int)min(32LL, (long long)n - r0);
+    const int start = lane < nr ? __ldg(rowptr + r0 + lane) : INT_MAX;
+    const int eb = __shfl_sync(kFullMask, start, 0);
+    const int ee = __ldg(rowptr + r0 + nr);
+    for (int kb = eb; kb < ee; kb += 32) {
+        const int k = kb + lane;
+        const int l = group_row_of(start, k, nr);
+        if (k < ee) {
+            T yi[NR], xr[NR];
+            load_rhs<T, NR, VEC>(own + (size_t)(r0 + l) * ld, nrhs, yi);
+            load_rhs<T, NR, VEC>(other + (size_t)__ldg(colidx + k) * ld, nrhs, xr);
+            T acc = T(0);
 #pragma unroll
-        for (int q = 0; q < NR; ++q)
-            acc = fma(yi[q], xr[q], acc);
-        grad[k] = accumulate ? grad[k] - acc : -acc;
+            for (int q = 0; q < NR; ++q)
+                acc = fma(yi[q], xr[q], acc);
+            grad[k] = accumulate ? grad[k] - acc : -acc;
+        }
     }
 }
 
@@ -455,7 +465,7 @@ template <typename T, int NR>
 static cudaError_t launch_grad_nr(const int *rowptr, const int *colidx, const T *own, const T *other, T *grad,
                                   int n, int nrhs, long long ld, int accumulate, cudaStream_t st)
 {
-    const unsigned blocks = (unsigned)(((long long)n + 255) / 256);
+    const unsigned blocks = (unsigned)(((long long)n + 255) / 256);  // a warp per 32 rows
     const int w = Vec16<T>::W;
     const bool vec = NR % w == 0 && nrhs == NR && ld % w == 0 && ((uintptr_t)own & 15) == 0 &&
                      ((uintptr_t)other & 15) == 0;

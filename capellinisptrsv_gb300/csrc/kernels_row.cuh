@@ -985,22 +985,43 @@ cudaError_t launch_fill_pending(T *x, int n, int nrhs, long long ld, unsigned *t
 // level-schedule values
 // ---------------------------------------------------------------------------
 
+// Level-schedule values: linv[p] = 1/d_p and, for every dependency k of
+// position p, lval[k] = -val[dep_src[k]] / d_p.  A warp takes 32 consecutive
+// positions (lane l computes position l's 1/d) and walks their dependencies
+// one per lane, each taking its position's 1/d from the owning lane, so the
+// reads of dep_src and the writes of lval are coalesced.
 template <typename T>
-__global__ void level_values_kernel(const int *__restrict__ lptr, const int *__restrict__ dep_src,
-                                    const int *__restrict__ diag_src, int n, const T *__restrict__ val,
-                                    T *__restrict__ lval, T *__restrict__ linv, int *bad)
+__global__ void __launch_bounds__(256) level_values_kernel(const int *__restrict__ lptr,
+                                                           const int *__restrict__ dep_src,
+                                                           const int *__restrict__ diag_src, int n,
+                                                           const T *__restrict__ val, T *__restrict__ lval,
+                                                           T *__restrict__ linv, int *bad)
 {
-    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long p = tid; p < n; p += stride) {
-        const T dg = val[diag_src[p]];
-        if (!(dg != T(0)) || !isfinite(dg))
-            atomicMin(bad, (int)p);
-        const T d = T(1) / dg;
-        linv[p] = d;
-        // pre-scaled dependencies: x_p = b/d_p + sum (-v/d_p) x_q
-        for (int k = lptr[p]; k < lptr[p + 1]; ++k)
-            lval[k] = -val[dep_src[k]] * d;
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long p0 = warp * 32; p0 < n; p0 += nwarps * 32) {
+        const int nr = (int)min(32LL, (long long)n - p0);
+        T d = T(0);
+        int start = INT_MAX;
+        if (lane < nr) {
+            const T dg = val[diag_src[p0 + lane]];
+            if (!(dg != T(0)) || !isfinite(dg))
+                atomicMin(bad, (int)(p0 + lane));
+            d = T(1) / dg;
+            linv[p0 + lane] = d;
+            start = lptr[p0 + lane];
+        }
+        const int eb = __shfl_sync(kFullMask, start, 0);
+        const int ee = lptr[p0 + nr];
+        for (int kb = eb; kb < ee; kb += 32) {
+            const int k = kb + lane;
+            const int l = group_row_of(start, k, nr);
+            const T dl = __shfl_sync(kFullMask, d, l);
+            // pre-scaled dependencies: x_p = b/d_p + sum (-v/d_p) x_q
+            if (k < ee)
+                lval[k] = -val[dep_src[k]] * dl;
+        }
     }
 }
 
@@ -1008,9 +1029,9 @@ template <typename T>
 cudaError_t launch_level_values(const int *lptr, const int *dep_src, const int *diag_src, int n,
                                 const T *val, T *lval, T *linv, int *bad, cudaStream_t st)
 {
-    long long blocks = ((long long)n + 255) / 256;
-    if (blocks > 8192)
-        blocks = 8192;
+    long long blocks = ((long long)n + 255) / 256;  // a warp per 32 positions
+    if (blocks > 16384)
+        blocks = 16384;
     if (blocks < 1)
         blocks = 1;
     level_values_kernel<T><<<(unsigned)blocks, 256, 0, st>>>(lptr, dep_src, diag_src, n, val, lval, linv, bad);

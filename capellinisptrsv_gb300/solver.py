@@ -299,6 +299,12 @@ class TriangularSolver:
             self._val_key = (val.data_ptr(), val._version)
         N.check(N.lib.capsp_refresh_values(self._h, _ptr(val), C.c_void_p(_current_stream(stream))))
 
+    def refresh_values_if_rebound(self, val, stream=None) -> None:
+        """refresh_values(val) unless `val` is the tensor, at the version, that the
+        solver's latest refresh or set_values bound."""
+        if (val.data_ptr(), val._version) != self._val_key:
+            self.refresh_values(val, stream)
+
     # -- vectors --------------------------------------------------------------
     def _vec(self, t, name):
         if not (torch is not None and isinstance(t, torch.Tensor) and t.is_cuda):

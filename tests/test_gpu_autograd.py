@@ -1,7 +1,9 @@
 """Differentiation form: torch.autograd.Function whose backward is the
-column-driven transpose solve fused with grad_val.  Checked against the serial
-host adjoint (oracle BACKWARD executor), against central finite differences
-along random directions (h = 1e-6), and with torch.autograd.gradcheck."""
+transpose solve over the solver's transposed view plus the grad_val pass (or,
+under "syncfree_csc", the column-driven transpose with grad_val fused).
+Checked against the serial host adjoint (oracle BACKWARD executor), against
+central finite differences along random directions (h = 1e-6), and with
+torch.autograd.gradcheck."""
 from __future__ import annotations
 
 import numpy as np
@@ -104,3 +106,23 @@ def test_module_with_parameter_trains():
         opt.step()
         losses.append(float(loss.detach()))
     assert losses[-1] < losses[0]
+
+
+def test_two_forwards_share_a_solver():
+    """Two forwards through one solver with different value tensors, then one
+    backward: each backward must solve with its own forward's values (the
+    solver is re-bound to them when another forward re-bound it since)."""
+    m = cs.generate(n=20_000, kmin=1, kmax=6, band=500, seed=9)
+    k = 4
+    b = np.random.default_rng(3).standard_normal((m.n, k))
+    v1, v2 = m.val, m.val * 1.25
+    val1, val2 = t(v1, True), t(v2, True)
+    solver = cs.TriangularSolver(t(m.rowptr), t(m.colidx), val1.detach())
+    x1 = cs.sptrsv(solver, val1, t(b))
+    x2 = cs.sptrsv(solver, val2, t(b))
+    loss = (x1 ** 2).sum() + 3.0 * x2.sum()
+    loss.backward()
+    for v, val, g in ((v1, val1, 2.0 * x1.detach().cpu().numpy()), (v2, val2, np.full((m.n, k), 3.0))):
+        xo = oracle.solve_csr_lower(m.rowptr, m.colidx, v, b)
+        yo = oracle.solve_csr_transpose(m.rowptr, m.colidx, v, g)
+        assert rel_inf_err(val.grad.cpu().numpy(), oracle.grad_val(m.rowptr, m.colidx, yo, xo)) <= 1e-12
