@@ -6,6 +6,7 @@
 #include "capsp_internal.h"
 #include "graph_cache.h"
 
+#include <atomic>
 #include <chrono>
 #include <climits>
 #include <cmath>
@@ -92,6 +93,9 @@ struct RowView {
     int *d_perm = nullptr, *d_lptr = nullptr, *d_lidx = nullptr, *d_lsrc = nullptr, *d_dsrc = nullptr;
     void *d_lval = nullptr, *d_linv = nullptr;
     std::vector<int> h_lcum;  // lptr[k] + k: row-count prefix in position space (mix tables)
+    // capsp_solve_host's b upload: highest b segment per 32 positions (kernel: b_group_seg)
+    unsigned char *d_group_seg = nullptr;
+    long long group_seg_b0 = 0;  // first segment's rows the table was built for
 };
 
 // Which operations a handle solves through which view: the plain solve of a
@@ -156,6 +160,14 @@ struct capsp_handle_s {
     void *d_stage = nullptr;
     size_t stage_bytes = 0;
     cudaStream_t stage_stream = nullptr;
+    // capsp_solve_host uploads b and copies finished row segments of x back
+    // while the solve runs
+    cudaStream_t copy_stream = nullptr, upload_stream = nullptr;
+    cudaEvent_t ev_seg0 = nullptr, ev_seg1 = nullptr, ev_up = nullptr;
+    int *d_seg = nullptr;            // kMaxSegments completion counters, then kMaxSegments b flags
+    int *seg_req = nullptr;          // counters the next level launch counts into (nullptr: none)
+    const int *bready_req = nullptr; // b flags the next level launch waits on (nullptr: none)
+    int seg_req_rows = 0;            // ... rows per segment of x
     double analyse_ms = 0.0;
     bool profiling = false;
     cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;
@@ -209,10 +221,22 @@ static void free_handle(capsp_handle_t h)
         cudaFree(rv.d_dsrc);
         cudaFree(rv.d_lval);
         cudaFree(rv.d_linv);
+        cudaFree(rv.d_group_seg);
     }
     cudaFree(h->d_xp);
     if (h->stage_stream)
         cudaStreamDestroy(h->stage_stream);
+    if (h->copy_stream)
+        cudaStreamDestroy(h->copy_stream);
+    if (h->upload_stream)
+        cudaStreamDestroy(h->upload_stream);
+    if (h->ev_seg0)
+        cudaEventDestroy(h->ev_seg0);
+    if (h->ev_seg1)
+        cudaEventDestroy(h->ev_seg1);
+    if (h->ev_up)
+        cudaEventDestroy(h->ev_up);
+    cudaFree(h->d_seg);
     if (h->ev_k0)
         cudaEventDestroy(h->ev_k0);
     if (h->ev_k1)
@@ -998,6 +1022,12 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, int v, const T *b, T *x, in
         a.win_base = nullptr;
         a.win_bytes = 0;
         a.win_hit = 0.f;
+        // rows are complete once the launch of the last right-hand sides ends
+        const bool count = level && h->seg_req != nullptr && r0 + nb == nrhs;
+        a.seg_count = count ? h->seg_req : nullptr;
+        a.b_ready = level && rv.d_group_seg ? h->bready_req : nullptr;
+        a.b_group_seg = a.b_ready ? rv.d_group_seg : nullptr;
+        a.seg_rows = count ? h->seg_req_rows : 1;
         if (level && h->l2_mode != CAPSP_L2_HINTS && h->l2_window > 0) {
             const size_t bytes = h->vbytes * (size_t)h->n * (size_t)nb;
             a.win_base = h->d_xp;
@@ -1257,6 +1287,71 @@ static void *pinned_alias(const void *p, int device)
     return at.devicePointer;
 }
 
+// cuStreamWaitValue32 / cuStreamWriteValue32 from the driver, or nullptr
+// where the driver has no stream memory operations (then capsp_solve_host
+// uploads b before the solve and copies x after it)
+typedef int (*StreamValue32Fn)(cudaStream_t, unsigned long long, unsigned int, unsigned int);
+static std::atomic<bool> g_stream_value_failed{false};
+static StreamValue32Fn driver_stream_value32(const char *name)
+{
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return reinterpret_cast<StreamValue32Fn>(p);
+}
+static StreamValue32Fn wait_value32()
+{
+    static const StreamValue32Fn fn = driver_stream_value32("cuStreamWaitValue32");
+    return g_stream_value_failed.load() ? nullptr : fn;
+}
+static StreamValue32Fn write_value32()
+{
+    static const StreamValue32Fn fn = driver_stream_value32("cuStreamWriteValue32");
+    return g_stream_value_failed.load() ? nullptr : fn;
+}
+
+// Highest b segment (segments of b0 (2^k - 1) .. b0 (2^(k+1) - 1) rows) among
+// the rows of every 32 schedule positions of view v; built once per handle
+static capsp_status_t ensure_b_groups(capsp_handle_t h, int v, long long b0)
+{
+    RowView &rv = h->view[v];
+    if (rv.d_group_seg != nullptr && rv.group_seg_b0 == b0)
+        return CAPSP_OK;
+    const int n = h->n, ng = (n + 31) / 32;
+    std::vector<int> perm((size_t)n);
+    CAPSP_CUDA(cudaMemcpy(perm.data(), rv.d_perm, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
+    std::vector<unsigned char> grp((size_t)ng, 0);
+    for (int p = 0; p < n; ++p) {
+        unsigned long long q = (unsigned long long)(perm[(size_t)p] / b0) + 1ull;
+        unsigned char k = 0;
+        while (q > 1ull) {
+            q >>= 1;
+            ++k;
+        }
+        if (k > grp[(size_t)p >> 5])
+            grp[(size_t)p >> 5] = k;
+    }
+    if (rv.d_group_seg == nullptr)
+        CAPSP_CUDA(cudaMalloc(&rv.d_group_seg, (size_t)ng));
+    CAPSP_CUDA(cudaMemcpy(rv.d_group_seg, grp.data(), (size_t)ng, cudaMemcpyHostToDevice));
+    rv.group_seg_b0 = b0;
+    return CAPSP_OK;
+}
+
+// Copies of x that overlap the solve: rows finish roughly in index order on
+// banded matrices (wide_4m: with 32 segments of rows, segment s is complete
+// at about 0.1 + 0.9 s/32 of the level chain), so each segment goes to the
+// host as soon as the kernel has counted all its rows.  Segments of at least
+// 64k rows, at most 32 of them.
+constexpr int kMaxSegments = 32;
+constexpr int kSegmentRowsMin = 65536;
+constexpr unsigned kWaitValueGeq = 0u;   // CU_STREAM_WAIT_VALUE_GEQ
+constexpr unsigned kWriteValueFenced = 0u; // CU_STREAM_WRITE_VALUE_DEFAULT: prior copies visible first
+
 extern "C" capsp_status_t capsp_solve_host(capsp_handle_t h, const void *b_host, void *x_host, int nrhs)
 {
     CAPSP_TRY(check_vec_args(h, b_host, x_host, nrhs, nrhs));
@@ -1274,12 +1369,12 @@ extern "C" capsp_status_t capsp_solve_host(capsp_handle_t h, const void *b_host,
     }
     char *db = (char *)h->d_stage, *dx = db + bytes;
     cudaStream_t st = h->stage_stream;
-    // A page-locked b is read in place on the level schedule: the row kernel
-    // reads each b element once, at row set-up, off the dependency chain, over
-    // the coherent CPU-GPU link, so the H2D copy disappears (measured on
-    // GB300 + Grace: wide_4m e2e 1.14 -> 1.05 ms).  x stays staged: the rows
-    // finish scattered over x, and scattered stores to host memory were
-    // slower than one D2H copy (1.49 ms).  Levels of 32k rows and more keep
+    // Up to 64k rows: a page-locked b is read in place on the level schedule:
+    // the row kernel reads each b element once, at row set-up, off the
+    // dependency chain, over the coherent CPU-GPU link, so the H2D copy
+    // disappears.  x stays staged: the rows finish scattered over x, and
+    // scattered stores to host memory were slower than one D2H copy (wide_4m:
+    // 1.49 ms).  Larger systems take the segmented copies below.  Levels of 32k rows and more keep
     // the GPU busy without waiting, and then a single right-hand side, 8 bytes
     // per scattered read over the link, costs more than the copy (2,048
     // systems with 93k rows per level: 5.66 ms in place, 4.80 ms copied; with
@@ -1288,13 +1383,104 @@ extern "C" capsp_status_t capsp_solve_host(capsp_handle_t h, const void *b_host,
     void *b_in_place = (!column_driven(h, kOpSolve) && view_level(h, v) && !(wide_levels(h, v) && nrhs == 1))
                            ? pinned_alias(b_host, h->device)
                            : nullptr;
-    if (b_in_place) {
-        CAPSP_TRY(dispatch(h, kOpSolve, b_in_place, dx, nullptr, nullptr, nrhs, nrhs, st));
+    const long long nseg_want = ((long long)h->n + kSegmentRowsMin - 1) / kSegmentRowsMin;
+    const Tuning tn = current_tuning(h, kOpSolve, nrhs);
+    const bool progressive = !column_driven(h, kOpSolve) && view_level(h, v) && nseg_want >= 2 &&
+                             row_hostio_supported(tn.kind < 0 ? kRowWrtFst : tn.kind, tn.R, nrhs) &&
+                             wait_value32() != nullptr && pinned_alias(x_host, h->device) != nullptr;
+    if (!progressive) {
+        if (b_in_place) {
+            CAPSP_TRY(dispatch(h, kOpSolve, b_in_place, dx, nullptr, nullptr, nrhs, nrhs, st));
+        } else {
+            CAPSP_CUDA(cudaMemcpyAsync(db, b_host, bytes, cudaMemcpyHostToDevice, st));
+            CAPSP_TRY(dispatch(h, kOpSolve, db, dx, nullptr, nullptr, nrhs, nrhs, st));
+        }
+        CAPSP_CUDA(cudaMemcpyAsync(x_host, dx, bytes, cudaMemcpyDeviceToHost, st));
+        return capsp_status_sync(h, st);
+    }
+    if (!h->copy_stream) {
+        CAPSP_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        CAPSP_CUDA(cudaStreamCreateWithFlags(&h->upload_stream, cudaStreamNonBlocking));
+    }
+    if (!h->ev_seg0) {
+        CAPSP_CUDA(cudaEventCreateWithFlags(&h->ev_seg0, cudaEventDisableTiming));
+        CAPSP_CUDA(cudaEventCreateWithFlags(&h->ev_seg1, cudaEventDisableTiming));
+        CAPSP_CUDA(cudaEventCreateWithFlags(&h->ev_up, cudaEventDisableTiming));
+    }
+    if (!h->d_seg)
+        CAPSP_CUDA(cudaMalloc(&h->d_seg, sizeof(int) * 2 * kMaxSegments));
+    int *d_count = h->d_seg, *d_bready = h->d_seg + kMaxSegments;
+    const int nseg0 = nseg_want < kMaxSegments ? (int)nseg_want : kMaxSegments;
+    // a multiple of 16 rows: no 128-byte line of b or x spans two segments
+    const int seg_rows = (int)((((long long)h->n + nseg0 - 1) / nseg0 + 15) / 16 * 16);
+    const int nseg = (int)(((long long)h->n + seg_rows - 1) / seg_rows);
+    const size_t row_bytes = h->vbytes * (size_t)nrhs;
+    CAPSP_CUDA(cudaMemsetAsync(h->d_seg, 0, sizeof(int) * 2 * kMaxSegments, st));
+    CAPSP_CUDA(cudaEventRecord(h->ev_seg0, st));
+    // b: a page-locked b goes up segment by segment on its own stream, each
+    // segment followed by its flag, and every row's set-up waits for its
+    // segment's flag, so the upload overlaps the solve (reading b in place
+    // over the link instead slowed the wide_4m kernel from 0.73 to 0.92 ms
+    // when x was coming back at the same time).  The upload is enqueued
+    // before the solve, so it never queues behind it; its segments double
+    // from n/256 rows, so the first lands within a microsecond and the host
+    // issues few calls before the launch.
+    const StreamValue32Fn write_fn = write_value32(), wait_fn = wait_value32();
+    const bool side_upload = pinned_alias(b_host, h->device) != nullptr && write_fn != nullptr;
+    bool b_flags = side_upload;
+    const long long b0 = ((h->n / 256 > 1024 ? h->n / 256 : 1024) + 15) / 16 * 16;
+    if (side_upload)
+        CAPSP_TRY(ensure_b_groups(h, v, b0));
+    if (side_upload) {
+        CAPSP_CUDA(cudaStreamWaitEvent(h->upload_stream, h->ev_seg0, 0));
+        for (int sg = 0; b0 * ((1LL << sg) - 1) < h->n; ++sg) {
+            const long long r0 = b0 * ((1LL << sg) - 1);
+            const long long r1 = b0 * ((1LL << (sg + 1)) - 1) < h->n ? b0 * ((1LL << (sg + 1)) - 1) : h->n;
+            CAPSP_CUDA(cudaMemcpyAsync(db + (size_t)r0 * row_bytes, (const char *)b_host + (size_t)r0 * row_bytes,
+                                       (size_t)(r1 - r0) * row_bytes, cudaMemcpyHostToDevice, h->upload_stream));
+            if (b_flags && write_fn(h->upload_stream, (unsigned long long)(uintptr_t)(d_bready + sg), 1u,
+                                    kWriteValueFenced) != 0) {
+                g_stream_value_failed.store(true);
+                b_flags = false;  // the solve waits for the whole upload instead
+            }
+        }
+        CAPSP_CUDA(cudaEventRecord(h->ev_up, h->upload_stream));
+        if (!b_flags)
+            CAPSP_CUDA(cudaStreamWaitEvent(st, h->ev_up, 0));
     } else {
         CAPSP_CUDA(cudaMemcpyAsync(db, b_host, bytes, cudaMemcpyHostToDevice, st));
-        CAPSP_TRY(dispatch(h, kOpSolve, db, dx, nullptr, nullptr, nrhs, nrhs, st));
     }
-    CAPSP_CUDA(cudaMemcpyAsync(x_host, dx, bytes, cudaMemcpyDeviceToHost, st));
+    h->seg_req = d_count;
+    h->bready_req = b_flags ? d_bready : nullptr;
+    h->seg_req_rows = seg_rows;
+    const capsp_status_t sd = dispatch(h, kOpSolve, db, dx, nullptr, nullptr, nrhs, nrhs, st);
+    h->seg_req = nullptr;
+    h->bready_req = nullptr;
+    if (side_upload)
+        CAPSP_CUDA(cudaStreamWaitEvent(st, h->ev_up, 0));  // db is free again once st is done
+    CAPSP_TRY(sd);
+    // once the solve has ended every counter is past its target, whatever it
+    // counted: no wait below can outlive the kernel.  This is enqueued on the
+    // solve's stream before any wait, so it cannot queue behind one.
+    CAPSP_CUDA(cudaMemsetAsync(d_count, 0x3F, sizeof(int) * (size_t)nseg, st));
+    CAPSP_CUDA(cudaStreamWaitEvent(h->copy_stream, h->ev_seg0, 0));
+    bool waits = true;
+    for (int sg = 0; sg < nseg; ++sg) {
+        const long long r0 = (long long)sg * seg_rows;
+        const long long r1 = r0 + seg_rows < h->n ? r0 + seg_rows : h->n;
+        if (waits && (wait_fn == nullptr || wait_fn(h->copy_stream, (unsigned long long)(uintptr_t)(d_count + sg),
+                                                    (unsigned)(r1 - r0), kWaitValueGeq) != 0)) {
+            // no stream memory operations after all: the other copies follow the solve
+            g_stream_value_failed.store(true);
+            waits = false;
+            CAPSP_CUDA(cudaEventRecord(h->ev_seg1, st));
+            CAPSP_CUDA(cudaStreamWaitEvent(h->copy_stream, h->ev_seg1, 0));
+        }
+        CAPSP_CUDA(cudaMemcpyAsync((char *)x_host + (size_t)r0 * row_bytes, dx + (size_t)r0 * row_bytes,
+                                   (size_t)(r1 - r0) * row_bytes, cudaMemcpyDeviceToHost, h->copy_stream));
+    }
+    CAPSP_CUDA(cudaEventRecord(h->ev_seg1, h->copy_stream));
+    CAPSP_CUDA(cudaStreamWaitEvent(st, h->ev_seg1, 0));
     return capsp_status_sync(h, st);
 }
 

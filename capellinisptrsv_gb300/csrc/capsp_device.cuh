@@ -53,6 +53,13 @@ __device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long lon
     return v;
 }
 
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p)
+{
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
 __device__ __forceinline__ unsigned int ld_relaxed(const unsigned int *p)
 {
     unsigned int v;

@@ -52,6 +52,18 @@ struct RowArgs {
     void *win_base;
     size_t win_bytes;
     float win_hit;
+    // level schedule: completion counters of the row segments of x, rows
+    // [s*seg_rows, (s+1)*seg_rows) counted into seg_count[s] as they finish
+    // (a copy stream waits on them); seg_count == nullptr: not counted
+    int *seg_count;
+    int seg_rows;
+    // level schedule: b_ready[k] != 0 once a copy stream has put b's rows of
+    // segment k in place; nullptr: b is resident.  Segments double: k covers
+    // rows [b0 (2^k - 1), b0 (2^(k+1) - 1)).  b_group_seg[q] is the highest
+    // segment of the rows at positions [32q, 32q + 32): a warp waits for that
+    // flag before it starts a chunk there (flags are set in segment order).
+    const int *b_ready;
+    const unsigned char *b_group_seg;
 };
 
 // Arguments of the column-driven solve (SyncFree CSC kernel, and the
@@ -93,6 +105,14 @@ inline int lanes_for_rhs(int nrhs)
     while (g < nrhs && g < 32)
         g <<= 1;
     return g;
+}
+
+// Launches that capsp_solve_host can overlap with its copies (a b_ready /
+// seg_count launch): one right-hand side, one row per lane, write-first or
+// mixed, level schedule, without the register cap
+inline bool row_hostio_supported(int kind, int rows_per_thread, int nrhs)
+{
+    return nrhs == 1 && rows_per_thread == 1 && (kind == kRowWrtFst || kind == kRowMix);
 }
 
 // regcap: the 64-register build of the multi-RHS write-first level kernel;

@@ -190,7 +190,38 @@ static_assert(staging_aligned<double>() && staging_aligned<float>(), "shared-mem
 // warp-wide DFMA occupies an SM sub-partition's FP64 pipe for ~64 cycles).
 // TWO (the two-phase schedule of the reference's our2Part) polls the outside
 // dependencies one at a time in storage order.
-template <typename T, int G, bool TWO, bool LEVEL, int RPL, bool STAGE>
+// b's element (i, r).  HOSTIO launches (capsp_solve_host) may run while a
+// copy stream is still uploading b: there b is read at gpu scope (the warp
+// has waited for the row's segment), past the non-coherent path.
+template <typename T, bool HOSTIO>
+__device__ __forceinline__ T load_b(const RowArgs<T> &a, int i, int r, unsigned long long pol)
+{
+    typedef typename VBits<T>::U U;
+    const T *p = a.b + (size_t)i * (size_t)a.ld + r;
+    if (HOSTIO && a.b_ready != nullptr)
+        return VBits<T>::from(ld_relaxed(reinterpret_cast<const U *>(p), pol));
+    return ld_stream(p, pol);
+}
+
+// While a copy stream is uploading b: wait (bounded) until every row of the
+// positions [lo, hi) has its b in place.  One flag per chunk, polled by lane 0.
+template <typename T>
+__device__ __forceinline__ void wait_b_chunk(const RowArgs<T> &a, int lo, int hi)
+{
+    const int lane = threadIdx.x & 31;
+    const int q0 = lo >> 5, q1 = (hi - 1) >> 5;
+    const int seg = __reduce_max_sync(kFullMask, q0 + lane <= q1 ? (int)a.b_group_seg[q0 + lane] : 0);
+    if (lane == 0) {
+        const unsigned *f = reinterpret_cast<const unsigned *>(a.b_ready + seg);
+        Spin sp;
+        while (ld_acquire(f) == 0u)
+            if (sp.next(a.err, a.wait, lo, -1))
+                break;
+    }
+    __syncwarp();
+}
+
+template <typename T, int G, bool TWO, bool LEVEL, int RPL, bool STAGE, bool HOSTIO>
 __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, const int sub, const int p,
                                            const bool mine, const int g,
                                            volatile typename VBits<T>::U *cache, const Slots<T> &sl,
@@ -229,7 +260,7 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
 #pragma unroll
         for (int r = 0; r < RPL; ++r) {
             if (has_rhs(r))
-                bi[r] = ld_stream(a.b + (size_t)i * (size_t)a.ld + r0 + r, pol.stream);
+                bi[r] = load_b<T, HOSTIO>(a, i, r0 + r, pol.stream);
             if (LEVEL)
                 acc[r] = bi[r] * dinv;  // x = b/d + sum (-v/d) x_j
         }
@@ -550,7 +581,7 @@ __device__ __forceinline__ void chunk_rows(const RowArgs<T> &a, const int lo, co
 // One heavy row per warp: 32/G slices of the row's entries x G right-hand
 // sides, advanced in convergent rounds; slices are reduced with butterfly
 // shuffles once every lane has consumed its entries.
-template <typename T, int G, bool LEVEL>
+template <typename T, int G, bool LEVEL, bool HOSTIO>
 __device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const int sl_idx, const int g,
                                          const Slots<T> &sl, const L2Pol &pol)
 {
@@ -575,7 +606,7 @@ __device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const
     T bi = T(0), v_last = T(0);
     int c_last = 0;
     if (owner) {
-        bi = ld_stream(a.b + (size_t)i * (size_t)a.ld + g, pol.stream);
+        bi = load_b<T, HOSTIO>(a, i, g, pol.stream);
         if (has_last) {
             c_last = ld_stream(rv.idx + j_last, pol.stream);
             v_last = ld_stream(rv.val + j_last, pol.stream);
@@ -695,13 +726,38 @@ __device__ __forceinline__ void warp_row(const RowArgs<T> &a, const int p, const
     }
 }
 
+// After the positions [lo, hi) of a warp's chunk have finished, count their
+// rows into the completion counters of their row segments: one atomic per
+// segment present in the chunk, after a fence that makes the chunk's stores
+// of x visible device-wide, so a copy that waits for a segment's full count
+// reads finished rows only.
+template <typename T>
+__device__ __forceinline__ void count_finished_rows(const RowArgs<T> &a, int lo, int hi)
+{
+    const int lane = threadIdx.x & 31;
+    __threadfence();
+    __syncwarp();
+    for (int base = lo; base < hi; base += 32) {
+        const int p = base + lane;
+        const int seg = p < hi ? __ldg(a.perm + p) / a.seg_rows : -1;
+        const unsigned grp = __match_any_sync(kFullMask, seg);
+        if (seg >= 0 && lane == __ffs(grp) - 1)
+            atomicAdd(a.seg_count + seg, __popc(grp));
+    }
+}
+
 // CAP limits registers to 64 so that every warp an SM can hold fits: with G >= 4
 // lanes per row on wide levels a warp holds few rows and residency decides
 // (measured on GB300: 16 RHS on wide_4m 2.55 -> 1.84 ms).  Narrow levels and
 // one or two lanes per row run faster with the full register budget.
 // RPL: right-hand sides per lane (G lanes per row cover G * RPL of them), so a
 // warp holds 32 / G rows however many right-hand sides there are.
-template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false, int RPL = 1, bool STAGE = false>
+// HOSTIO: a capsp_solve_host launch (one lane per row, level schedule): it
+// waits for b's segments while a copy stream uploads them and counts finished
+// rows per segment of x for the copy stream that takes them back.  A separate
+// build, so that the other launches keep their registers.
+template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false, int RPL = 1, bool STAGE = false,
+          bool HOSTIO = false>
 __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const RowArgs<T> a)
 {
     typedef typename VBits<T>::U U;
@@ -738,6 +794,8 @@ __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const Row
             if (tk >= (unsigned)a.n)
                 break;
             const int lo = (int)tk;
+            if (HOSTIO && a.b_ready != nullptr)
+                wait_b_chunk(a, lo, min(lo + CH, a.n));
 #pragma unroll
             for (int r = 0; r < R * RPL; ++r)
                 cache[r * 32 + lane] = VBits<T>::kPending;
@@ -746,25 +804,31 @@ __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const Row
             for (int r = 0; r < R; ++r) {
                 const int sub = lo + r * RPW;
                 const int p = sub + rl;
-                chunk_rows<T, G, KIND == kRowTwoPart, LEVEL, RPL, STAGE>(a, lo, sub, p, p < a.n && g * RPL < a.nrhs, g,
-                                                                  cache, sl, t_pick, pol);
+                chunk_rows<T, G, KIND == kRowTwoPart, LEVEL, RPL, STAGE, HOSTIO>(
+                    a, lo, sub, p, p < a.n && g * RPL < a.nrhs, g, cache, sl, t_pick, pol);
             }
             __syncwarp();
+            if (HOSTIO && a.seg_count != nullptr)
+                count_finished_rows(a, lo, min(lo + CH, a.n));
         } else {
             if (tk + 1u >= (unsigned)a.table_len)
                 break;
             const int lo = ld_stream(a.table + tk, pol.stream), hi = ld_stream(a.table + tk + 1, pol.stream);
+            if (HOSTIO && a.b_ready != nullptr)
+                wait_b_chunk(a, lo, hi);
             if (hi - lo > 1) {
                 cache[lane] = VBits<T>::kPending;
                 __syncwarp();
                 const int p = lo + rl;
-                chunk_rows<T, G, false, LEVEL, 1, STAGE>(a, lo, lo, p, p < hi && g < a.nrhs, g, cache, sl, t_pick,
-                                                        pol);
+                chunk_rows<T, G, false, LEVEL, 1, STAGE, HOSTIO>(a, lo, lo, p, p < hi && g < a.nrhs, g, cache, sl,
+                                                                t_pick, pol);
                 __syncwarp();
             } else {
-                warp_row<T, G, LEVEL>(a, lo, rl, g, sl, pol);
+                warp_row<T, G, LEVEL, HOSTIO>(a, lo, rl, g, sl, pol);
             }
             __syncwarp();
+            if (HOSTIO && a.seg_count != nullptr)
+                count_finished_rows(a, lo, hi);
         }
     }
 }
@@ -773,12 +837,13 @@ __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const Row
 // launch helpers
 // ---------------------------------------------------------------------------
 
-template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false, int RPL = 1, bool STAGE = false>
+template <typename T, int G, int R, int KIND, bool LEVEL, bool CAP = false, int RPL = 1, bool STAGE = false,
+          bool HOSTIO = false>
 static cudaError_t launch_row_impl(const RowArgs<T> &a, int block, int bps, int num_sms,
                                    cudaStream_t st)
 {
     constexpr int RPW = 32 / G;
-    auto kern = row_solve_kernel<T, G, R, KIND, LEVEL, CAP, RPL, STAGE>;
+    auto kern = row_solve_kernel<T, G, R, KIND, LEVEL, CAP, RPL, STAGE, HOSTIO>;
     const size_t smem = (size_t)(block / 32) * warp_smem_bytes<T>(R, RPL, STAGE);
     cudaError_t e = cudaSuccess;
     if (smem > 48 * 1024) {
@@ -910,6 +975,22 @@ template <typename T>
 cudaError_t launch_row_solve(const RowArgs<T> &a, int kind, int rows_per_thread, int block,
                              int blocks_per_sm, int num_sms, bool regcap, bool stage, cudaStream_t st)
 {
+    if (a.b_ready != nullptr || a.seg_count != nullptr) {
+        if (a.perm == nullptr || regcap || !row_hostio_supported(kind, rows_per_thread, a.nrhs))
+            return cudaErrorNotSupported;
+        if constexpr (sizeof(T) == 8) {
+            if (stage)
+                return kind == kRowMix
+                           ? launch_row_impl<T, 1, 1, kRowMix, true, false, 1, true, true>(a, block, blocks_per_sm,
+                                                                                          num_sms, st)
+                           : launch_row_impl<T, 1, 1, kRowWrtFst, true, false, 1, true, true>(a, block, blocks_per_sm,
+                                                                                             num_sms, st);
+        }
+        return kind == kRowMix
+                   ? launch_row_impl<T, 1, 1, kRowMix, true, false, 1, false, true>(a, block, blocks_per_sm, num_sms, st)
+                   : launch_row_impl<T, 1, 1, kRowWrtFst, true, false, 1, false, true>(a, block, blocks_per_sm, num_sms,
+                                                                                      st);
+    }
     if (a.perm != nullptr)
         return launch_row_sched<T, true>(a, kind, rows_per_thread, block, blocks_per_sm, num_sms, regcap, stage,
                                          st);

@@ -253,8 +253,15 @@ capsp_status_t capsp_reserve(capsp_handle_t h, int max_nrhs);
  * solve on this handle (CAPSP_OK or CAPSP_ERR_TIMEOUT). */
 capsp_status_t capsp_status_sync(capsp_handle_t h, void *stream);
 
-/* Host-buffer convenience: copy b (host) in, solve, copy x (host) out,
- * synchronously.  Uses handle-owned pinned and device staging buffers. */
+/* Host-buffer solve: b (host) in, solve, x (host) out, synchronously, through
+ * handle-owned device staging buffers.  With page-locked b and x, one
+ * right-hand side and more than 64k rows on the level schedule, the copies
+ * overlap the solve: b goes up in doubling row segments on a second stream
+ * (each chunk of rows waits for its segment), and x comes back in up to 32
+ * segments, each as soon as the kernel has counted all its rows finished
+ * (stream memory operations, cuStreamWaitValue32 / cuStreamWriteValue32).
+ * Otherwise b is copied (or, up to 64k rows, read in place when page-locked)
+ * before the solve and x after it. */
 capsp_status_t capsp_solve_host(capsp_handle_t h, const void *b_host, void *x_host,
                                 int nrhs);
 
