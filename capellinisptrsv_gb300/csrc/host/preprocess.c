@@ -16,6 +16,10 @@
  * kernels_row.cuh) */
 #define CAPSP_ROW_PASS 8
 
+/* a level this wide keeps the GPU busy without waiting on the dependency
+ * chain (the launch-shape rule in capsp_api.cu uses the same width) */
+#define CAPSP_WIDE_LEVEL 32768
+
 /* ------------------------------------------------------------------ */
 /* small helpers                                                        */
 /* ------------------------------------------------------------------ */
@@ -172,21 +176,27 @@ int capsp_row_levels(int n, const int *rowptr, const int *colidx, int *level, in
  * level 1 + the deepest level among its dependencies, and the levels are laid
  * out one after another, giving order[k] (k-th row to solve) and
  * position[row] = k.  Any order that lists dependencies first keeps the
- * sync-free solve correct.  Inside a level, rows are ordered
- *   - in a level that holds a row of more than CAPSP_ROW_PASS dependencies
- *     (more than the row kernel takes in one pass), by dependency count, most
- *     first (counts of 63 and more share a bucket), then solve order: a warp's
- *     32 consecutive rows then need the same number of passes instead of all
- *     waiting for the longest (measured on GB300: 2,048 banded systems with
- *     3-12 dependencies per row, 1.96 -> 1.64 ms; 1M rows with 2-10, 1.38 ->
- *     1.35 ms);
- *   - in any other level, by the position of the row's newest dependency (the
- *     last to be published, as a rule), then solve order: a warp's 32 rows then
- *     wait on a few neighbouring rows of the previous level, published by one
- *     or two warps, so their polls share cache lines instead of reaching 32
- *     unrelated producers (measured on GB300: wide_4m 0.756 -> 0.742 ms, FP32
- *     0.694 -> 0.671 ms; applied to the multi-pass levels too, it cost the
- *     2,048 systems 1.4 % and 1M rows with 2-10 dependencies 1 %).
+ * sync-free solve correct.  Inside a level (then solve order):
+ *   - the rows of more than CAPSP_ROW_PASS dependencies (more than the row
+ *     kernel takes in one pass) come first, by dependency count, most first
+ *     (counts of 63 and more share a bucket): a warp's 32 consecutive rows then
+ *     need the same number of passes instead of all waiting for the longest
+ *     (measured on GB300: 2,048 banded systems with 3-12 dependencies per row,
+ *     1.96 -> 1.64 ms; 1M rows with 2-10, 1.38 -> 1.35 ms);
+ *   - the other rows follow by the position of their newest dependency (the
+ *     last to be published, as a rule): a warp's 32 rows then wait on a few
+ *     neighbouring rows of the previous level, published by one or two warps,
+ *     so their polls share cache lines instead of reaching 32 unrelated
+ *     producers (measured on GB300: wide_4m 0.756 -> 0.742 ms, FP32 0.694 ->
+ *     0.671 ms; with the multi-pass rows first instead of the whole level by
+ *     count: wide_4m's transpose, 2.4 % of whose rows take two passes, 0.928
+ *     -> 0.890 ms, 1M rows with 2-10 dependencies 1.301 -> 1.279 ms, its
+ *     transpose 1.352 -> 1.315 ms);
+ *   - except in a level of CAPSP_WIDE_LEVEL rows or more that holds a
+ *     multi-pass row, where all rows go by dependency count: there no warp
+ *     waits on the chain, and rows of equal work finish a warp's passes
+ *     together (the newest-dependency order for the single-pass rows cost the
+ *     2,048 systems, 93k rows per level, 3 %).
  * level_start (n+2 ints, optional) receives the first position of every level.
  * Returns the number of levels, or -1 on allocation failure. */
 int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *order, int *position,
@@ -237,7 +247,7 @@ int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *
      * dependency sets its level, and positions ascend with the level), so the
      * key of a single-pass level ranges over the previous level's positions. */
     int *tmp = lev; /* the row levels are no longer needed */
-    int *hist = (int *)malloc(sizeof(int) * ((size_t)(widest > 64 ? widest : 64) + 1));
+    int *hist = (int *)malloc(sizeof(int) * ((size_t)widest + 64 + 1));
     int *key = (int *)malloc(sizeof(int) * (size_t)(widest > 0 ? widest : 1));
     if (!hist || !key) {
         free(hist);
@@ -256,26 +266,31 @@ int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *
                 const int d = ptr[i + 1] - ptr[i] - 1;
                 most = d > most ? d : most;
             }
-            int base = 0, range;
-            if (most > CAPSP_ROW_PASS) {
-                /* bucket 0: 63+ dependencies ... bucket 63: none */
-                range = 64;
+            int range;
+            /* a level of 32k rows or more keeps the GPU busy without waiting:
+             * there rows of equal dependency count together finish a warp's
+             * passes together */
+            const int by_count = most > CAPSP_ROW_PASS && b - a >= CAPSP_WIDE_LEVEL;
+            if (l > 1) {
+                /* multi-pass rows first, by dependency count (bucket 0: 63+
+                 * dependencies), then the single-pass rows by the position
+                 * of their newest dependency (buckets 64 ...) */
+                const int base = cnt[l - 2];
+                range = by_count ? 64 : most > CAPSP_ROW_PASS ? 64 + (a - base) : a - base;
+                const int off = most > CAPSP_ROW_PASS ? 64 : 0;
                 for (int k = a; k < b; ++k) {
                     const int i = order[k];
                     const int d = ptr[i + 1] - ptr[i] - 1;
-                    key[k - a] = 63 - (d < 63 ? d : 63);
-                }
-            } else if (l > 1) {
-                base = cnt[l - 2];
-                range = a - base; /* the previous level's positions */
-                for (int k = a; k < b; ++k) {
-                    const int i = order[k];
+                    if (d > CAPSP_ROW_PASS || by_count) {
+                        key[k - a] = 63 - (d < 63 ? d : 63);
+                        continue;
+                    }
                     const int s = ptr[i] + (upper ? 1 : 0), e = ptr[i + 1] - (upper ? 0 : 1);
                     int newest = base;
                     for (int j = s; j < e; ++j)
                         if (position[idx[j]] > newest)
                             newest = position[idx[j]];
-                    key[k - a] = newest - base;
+                    key[k - a] = off + newest - base;
                 }
             } else {
                 range = 0; /* level 1: no dependencies, solve order */

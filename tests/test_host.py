@@ -212,25 +212,49 @@ def test_level_schedule_is_a_topological_level_order(upper):
     # levels are contiguous blocks of positions
     lev_of_pos = np.repeat(np.arange(1, levels + 1), np.diff(start[1:levels + 2]))
     assert np.all(np.diff(lev_of_pos) >= 0)
-    # inside a level holding a row of more than 8 dependencies (one pass of the
-    # row kernel): dependency count non-increasing (63+ in one bucket), then
-    # solve order; inside any other level: the position of the newest
-    # dependency, then solve order
+    # inside a level (all narrower than 32k rows here): the rows of more than 8
+    # dependencies (one pass of the row kernel) first, dependency count
+    # non-increasing (63+ in one bucket), then solve order; then the other
+    # rows by the position of their newest dependency, then solve order
+    _check_level_order(rp, order, dep_ptr, dep_idx, start, levels, upper, wide=32768)
+    ndep = np.diff(rp)[order] - 1
+    assert np.any(ndep > 8)
+
+
+def _check_level_order(rp, order, dep_ptr, dep_idx, start, levels, upper, wide):
+    n = len(order)
     ndep = np.minimum(np.diff(rp)[order] - 1, 63)
-    solve_rank = (m.n - 1 - order) if upper else order
+    solve_rank = (n - 1 - order) if upper else order
     newest = np.array([dep_idx[dep_ptr[k]:dep_ptr[k + 1]].max() if dep_ptr[k + 1] > dep_ptr[k] else -1
-                       for k in range(m.n)])
-    sorted_levels = 0
+                       for k in range(n)])
     for l in range(1, levels + 1):
         a, b = start[l], start[l + 1]
         d, key, r = ndep[a:b], newest[a:b], solve_rank[a:b]
-        multi = bool(d.size and d.max() > 8)
-        sorted_levels += multi
-        bucket = -d if multi else np.zeros_like(d)
-        key = np.zeros_like(key) if multi else key
-        triples = list(zip(bucket.tolist(), key.tolist(), r.tolist()))
-        assert triples == sorted(triples)
-    assert 0 < sorted_levels < levels
+        by_count = bool(d.size and d.max() > 8) and b - a >= wide
+        multi = (d > 8) | by_count
+        group = np.where(multi, 0, 1)
+        bucket = np.where(multi, -d, 0)
+        key = np.where(multi, 0, key)
+        rows = list(zip(group.tolist(), bucket.tolist(), key.tolist(), r.tolist()))
+        assert rows == sorted(rows), l
+
+
+def test_level_order_of_a_wide_level():
+    """A level of 32k rows or more that holds a multi-pass row is ordered by
+    dependency count alone (then solve order)."""
+    from capellinisptrsv_gb300.solver import level_layout, level_schedule
+    rng = np.random.default_rng(3)
+    n0, n1 = 100, 40_000  # level 1: rows 0..99; level 2: 40,000 rows on them
+    counts = np.concatenate([np.zeros(n0, np.int64), rng.integers(1, 13, n1)])
+    rp = np.concatenate([[0], np.cumsum(counts + 1)]).astype(np.int32)
+    ci = np.empty(rp[-1], np.int32)
+    for i in range(n0 + n1):
+        ci[rp[i]:rp[i + 1] - 1] = np.sort(rng.choice(n0, counts[i], replace=False)) if counts[i] else []
+        ci[rp[i + 1] - 1] = i
+    levels, order, pos, start = level_schedule(n0 + n1, rp, ci, False)
+    assert levels == 2 and start[3] - start[2] == n1
+    dep_ptr, dep_idx, _, _ = level_layout(n0 + n1, rp, ci, order, pos, False)
+    _check_level_order(rp, order, dep_ptr, dep_idx, start, levels, False, wide=32768)
 
 
 def _validate(rp, ci, fmt=N.FMT_CSR, uplo=N.LOWER):
