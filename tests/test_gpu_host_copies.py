@@ -78,3 +78,68 @@ def test_copy_after_solve_paths(banded, how):
     s.solve_host(b, x)
     assert rel_inf_err(x, oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)) <= TOL64
     s.close()
+
+
+def test_segmented_copies_mix_kernel(banded):
+    """The mixed kernel (heavy 32-row groups warp-per-row at border 4) with the
+    segmented copies: its warp-per-row chunks wait for b and count rows too."""
+    m = banded
+    s = cs.TriangularSolver(m.rowptr, m.colidx, m.val, algorithm="mix")
+    s.set_mix_border(4)
+    _, x = pinned(m.n, 0)
+    for seed in (7, 8):
+        _, b = pinned(m.n, seed)
+        s.solve_host(b, x)
+        assert rel_inf_err(x, oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, b)) <= TOL64
+    assert s.info()["warp_occupy"] > 0.0
+    s.close()
+
+
+def test_segmented_copies_fp32(banded):
+    m = banded
+    v32 = m.val.astype(np.float32)
+    s = cs.TriangularSolver(m.rowptr, m.colidx, v32)
+    xt = torch.empty(m.n, dtype=torch.float32).pin_memory()
+    bt = torch.from_numpy(np.random.default_rng(9).standard_normal(m.n).astype(np.float32)).pin_memory()
+    s.solve_host(bt.numpy(), xt.numpy())
+    xo = oracle.solve_csr_lower(m.rowptr, m.colidx, v32, bt.numpy())
+    assert rel_inf_err(xt.numpy(), xo) <= 1e-5
+    s.close()
+
+
+def test_segmented_copies_wide_levels():
+    """Ten levels of 40,000 rows (each row depends on 1-12 rows of the level
+    before): the launch for levels of 32k rows and more, with the copies."""
+    rng = np.random.default_rng(10)
+    nb, w = 10, 40_000
+    n = nb * w
+    counts = np.concatenate([np.zeros(w, np.int64), rng.integers(1, 13, n - w)])
+    # k distinct rows of the level before: base + t * step (mod w), t < k <= 12
+    base = rng.integers(0, w, n)
+    step = rng.integers(1, w // 12, n)
+    offs = np.sort((base[:, None] + np.arange(12)[None, :] * step[:, None]) % w, axis=1)
+    offs = np.where(np.arange(12)[None, :] < counts[:, None], offs, w)  # unused slots last
+    offs.sort(axis=1)
+    rows = np.arange(n)
+    lo = (rows // w - 1) * w
+    rp = np.concatenate([[0], np.cumsum(counts + 1)]).astype(np.int32)
+    ci = np.empty(rp[-1], np.int32)
+    val = np.empty(rp[-1])
+    used = np.arange(12)[None, :] < counts[:, None]
+    r_of = np.repeat(rows, counts)
+    dep_pos = (rp[:-1][:, None] + np.arange(12)[None, :])[used]
+    ci[dep_pos] = (lo[:, None] + offs)[used]
+    val[dep_pos] = rng.uniform(-1, 1, dep_pos.size)
+    diag = rp[1:] - 1
+    ci[diag] = rows
+    absum = np.zeros(n)
+    np.add.at(absum, r_of, np.abs(val[dep_pos]))
+    val[diag] = 1.0 + absum
+    s = cs.TriangularSolver(rp, ci, val)
+    assert s.info()["levels"] == nb
+    _, x = pinned(n, 0)
+    for seed in (11, 12):
+        _, b = pinned(n, seed)
+        s.solve_host(b, x)
+        assert rel_inf_err(x, oracle.solve_csr_lower(rp, ci, val, b)) <= TOL64
+    s.close()
