@@ -1369,26 +1369,28 @@ extern "C" capsp_status_t capsp_solve_host(capsp_handle_t h, const void *b_host,
     }
     char *db = (char *)h->d_stage, *dx = db + bytes;
     cudaStream_t st = h->stage_stream;
-    // Up to 64k rows: a page-locked b is read in place on the level schedule:
-    // the row kernel reads each b element once, at row set-up, off the
-    // dependency chain, over the coherent CPU-GPU link, so the H2D copy
-    // disappears.  x stays staged: the rows finish scattered over x, and
-    // scattered stores to host memory were slower than one D2H copy (wide_4m:
-    // 1.49 ms).  Larger systems take the segmented copies below.  Levels of 32k rows and more keep
-    // the GPU busy without waiting, and then a single right-hand side, 8 bytes
-    // per scattered read over the link, costs more than the copy (2,048
-    // systems with 93k rows per level: 5.66 ms in place, 4.80 ms copied; with
-    // 4 right-hand sides, 32 bytes per read, 8.97 ms in place, 11.2 copied).
     const int v = view_of(h, kOpSolve);
-    void *b_in_place = (!column_driven(h, kOpSolve) && view_level(h, v) && !(wide_levels(h, v) && nrhs == 1))
-                           ? pinned_alias(b_host, h->device)
-                           : nullptr;
     const long long nseg_want = ((long long)h->n + kSegmentRowsMin - 1) / kSegmentRowsMin;
     const Tuning tn = current_tuning(h, kOpSolve, nrhs);
     const bool progressive = !column_driven(h, kOpSolve) && view_level(h, v) && nseg_want >= 2 &&
                              row_hostio_supported(tn.kind < 0 ? kRowWrtFst : tn.kind, tn.R, nrhs) &&
                              wait_value32() != nullptr && pinned_alias(x_host, h->device) != nullptr;
     if (!progressive) {
+        // Copies before and after the solve.  A page-locked b is read in place
+        // on the level schedule: the row kernel reads each b element once, at
+        // row set-up, over the coherent CPU-GPU link, so the H2D copy
+        // disappears.  x stays staged: the rows finish scattered over x, and
+        // scattered stores to host memory were slower than one D2H copy
+        // (wide_4m: 1.49 ms).  Levels of 32k rows and more keep the GPU busy
+        // without waiting, and then a single right-hand side, 8 bytes per
+        // scattered read over the link, costs more than the copy (2,048
+        // systems with 93k rows per level: 5.66 ms in place, 4.80 ms copied;
+        // with 4 right-hand sides, 32 bytes per read, 8.97 ms in place, 11.2
+        // copied).
+        void *b_in_place =
+            (!column_driven(h, kOpSolve) && view_level(h, v) && !(wide_levels(h, v) && nrhs == 1))
+                ? pinned_alias(b_host, h->device)
+                : nullptr;
         if (b_in_place) {
             CAPSP_TRY(dispatch(h, kOpSolve, b_in_place, dx, nullptr, nullptr, nrhs, nrhs, st));
         } else {
@@ -1429,9 +1431,8 @@ extern "C" capsp_status_t capsp_solve_host(capsp_handle_t h, const void *b_host,
     const bool side_upload = pinned_alias(b_host, h->device) != nullptr && write_fn != nullptr;
     bool b_flags = side_upload;
     const long long b0 = ((h->n / 256 > 1024 ? h->n / 256 : 1024) + 15) / 16 * 16;
-    if (side_upload)
-        CAPSP_TRY(ensure_b_groups(h, v, b0));
     if (side_upload) {
+        CAPSP_TRY(ensure_b_groups(h, v, b0));
         CAPSP_CUDA(cudaStreamWaitEvent(h->upload_stream, h->ev_seg0, 0));
         for (int sg = 0; b0 * ((1LL << sg) - 1) < h->n; ++sg) {
             const long long r0 = b0 * ((1LL << sg) - 1);
