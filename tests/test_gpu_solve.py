@@ -495,3 +495,24 @@ def test_wide_levels_strided_multi_block_rhs(k, ld):
     xo = oracle.solve_csr_lower(m.rowptr, m.colidx, m.val, np.ascontiguousarray(b[:, :k]))
     assert rel_inf_err(x[:, :k].reshape(m.n, k), xo.reshape(m.n, k)) <= TOL64
     assert np.all(x[:, k:] == 7.0)  # columns past nrhs untouched
+
+
+@pytest.mark.parametrize("nrhs", [1, 4])
+def test_csc_transpose_grad(nrhs):
+    """The backward of a CSC handle: y = L^-T g over its stored columns (rows
+    of L^T), then grad_val over the CSC entries (column j, row idx[k]):
+    grad_val[k] = -sum_r y[idx[k], r] x[j, r]."""
+    m = cs.generate(n=20_000, kmin=1, kmax=9, band=800, seed=13)
+    cp, ri, cv = cs.matrix_transposition(m.n, m.n, m.nnz, m.rowptr, m.colidx, m.val)
+    shape = (m.n, nrhs) if nrhs > 1 else (m.n,)
+    g = np.random.default_rng(14).standard_normal(shape)
+    x = np.random.default_rng(15).standard_normal(shape)
+    yo = oracle.solve_csr_transpose(m.rowptr, m.colidx, m.val, g)
+    s = cs.TriangularSolver(dev(cp), dev(ri), dev(cv), fmt="csc")
+    y, gv = s.solve_transpose_grad(dev(g), dev(x))
+    s.status()
+    col = np.repeat(np.arange(m.n), np.diff(cp))
+    y2, x2 = yo.reshape(m.n, -1), x.reshape(m.n, -1)
+    go = -np.einsum("kr,kr->k", y2[ri], x2[col])
+    assert rel_inf_err(host(y), yo) <= TOL64
+    assert rel_inf_err(host(gv), go) <= TOL64
