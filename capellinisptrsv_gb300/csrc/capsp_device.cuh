@@ -53,6 +53,12 @@ __device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long lon
     return v;
 }
 
+// bring a global line into L2 (no register result, no ordering)
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p)
 {
     unsigned int v;
