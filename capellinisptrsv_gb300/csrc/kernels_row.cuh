@@ -798,8 +798,9 @@ __global__ void __launch_bounds__(512, (CAP ? 2 : 1)) row_solve_kernel(const Row
             // chunk that the warps will take one round from now, so its
             // set-up starts from L2 instead of DRAM (measured on GB300:
             // wide_4m 0.738 -> 0.724 ms, 2,048 systems 1.661 -> 1.653 ms,
-            // grad_1m 1.279 -> 1.268 ms; with 16 lanes per row it cost grad_1m
-            // 7 %, so multi-RHS launches do without).
+            // grad_1m 1.279 -> 1.268 ms; half a round or two rounds ahead gave
+            // the same to 0.3 %; with 16 lanes per row it cost grad_1m 7 %, so
+            // multi-RHS launches do without).
             if (LEVEL && G == 1) {
                 const long long ahead = (long long)lo + (long long)gridDim.x * (blockDim.x >> 5) * CH + lane;
                 if (ahead < a.n) {
