@@ -313,13 +313,22 @@ def test_upper_csr_and_csc_paths(schedule, path):
 
 
 def test_set_values_refreshes(plain20k):
+    """New values reach both views: the forward's and, once built, the
+    transposed view's level values."""
     m = plain20k
     s = solver_for(m)
     b = cs.normal(m.n, seed=7)
+    s.solve_transpose(dev(b))  # builds the transposed view with the old values
     v2 = m.val * 1.5
     s.set_values(dev(v2))
     xo = oracle.solve_csr_lower(m.rowptr, m.colidx, v2, b)
     assert rel_inf_err(host(s.solve(dev(b))), xo) <= TOL64
+    yo = oracle.solve_csr_transpose(m.rowptr, m.colidx, v2, b)
+    assert rel_inf_err(host(s.solve_transpose(dev(b))), yo) <= TOL64
+    v3 = m.val * 0.75
+    s.refresh_values(dev(v3))
+    yo = oracle.solve_csr_transpose(m.rowptr, m.colidx, v3, b)
+    assert rel_inf_err(host(s.solve_transpose(dev(b))), yo) <= TOL64
 
 
 def test_solve_host_buffers(plain20k):
