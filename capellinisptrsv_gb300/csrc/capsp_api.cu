@@ -864,9 +864,12 @@ static capsp_status_t ensure_column_order(capsp_handle_t h, int backward)
 // Launch shape of a row-path launch with nrhs right-hand sides.  Defaults
 // measured on GB300: with one lane per row (32 rows per warp) two resident
 // warps per SM suit narrow levels (more rows in flight than a few levels only
-// add pollers), twelve suit levels of 4k-32k rows (wide_4m, 5.8k rows per
+// add pollers), ten suit levels of 4k-32k rows (wide_4m, 5.8k rows per
 // level, warps per SM 2/4/6/8/12/16: 1.708/1.091/0.877/0.765/0.748/0.782 ms;
-// FP32 0.712 -> 0.694 ms at 12) and sixteen the levels of 32k rows and more,
+// with the L2 prefetch of the next round's metadata, 10 against 12 warps:
+// 0.718 against 0.727 ms, FP32 0.655 against 0.666 ms; the capsp_solve_host
+// build, whose chunks also wait for b and count their rows, keeps 12: 0.742
+// against 0.762 ms) and sixteen the levels of 32k rows and more,
 // which are bound by throughput (2,048 banded systems, 93k rows per level:
 // 2.95 ms at 8, 1.81 ms at 16); with G >= 4 lanes per row a warp holds few
 // rows, so every warp the SM can hold in 128-thread blocks pays off.
@@ -881,7 +884,7 @@ static bool wide_levels(capsp_handle_t h, int v)
 }
 
 static void row_shape(capsp_handle_t h, int v, const Tuning &tn, int nrhs, int *block, int *bps,
-                      bool *cap = nullptr)
+                      bool *cap = nullptr, bool hostio = false)
 {
     const int g = lanes_for_rhs(nrhs);
     const bool level = view_level(h, v);
@@ -893,7 +896,7 @@ static void row_shape(capsp_handle_t h, int v, const Tuning &tn, int nrhs, int *
     if (!tn.dflt)
         return;
     if (g == 1) {
-        *block = narrow ? 64 : (wide_levels(h, v) ? 512 : 384);
+        *block = narrow ? 64 : (wide_levels(h, v) ? 512 : (hostio ? 384 : 320));
         *bps = 1;
     } else if (g == 2) {
         *block = 256;
@@ -1040,7 +1043,7 @@ static capsp_status_t enqueue_rows(capsp_handle_t h, int v, const T *b, T *x, in
             CAPSP_CUDA(cudaEventRecord(h->ev_k0, st));
         int blk = 0, bps = 0;
         bool cap = false;
-        row_shape(h, v, tn, nb, &blk, &bps, &cap);
+        row_shape(h, v, tn, nb, &blk, &bps, &cap, a.seg_count != nullptr || a.b_ready != nullptr);
         // One lane per row stages each sub-chunk's entries in shared memory
         // with coalesced copies, which shortens the dependency hops of
         // latency-bound FP64 solves (measured on GB300: wide_4m 0.792 -> 0.771
