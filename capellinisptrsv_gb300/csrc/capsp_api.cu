@@ -862,9 +862,11 @@ static capsp_status_t ensure_column_order(capsp_handle_t h, int backward)
 }
 
 // Launch shape of a row-path launch with nrhs right-hand sides.  Defaults
-// measured on GB300: with one lane per row (32 rows per warp) two resident
+// measured on GB300: with one lane per row (32 rows per warp) four resident
 // warps per SM suit narrow levels (more rows in flight than a few levels only
-// add pollers), ten suit levels of 4k-32k rows (wide_4m, 5.8k rows per
+// add pollers; 4 against 2 warps: grad_1m 1.253 against 1.268 ms, its
+// transpose 1.296 against 1.314 ms, zipf40_1m 510 against 527 ms, zipf_1m
+// 100.7 against 100.3 ms), ten suit levels of 4k-32k rows (wide_4m, 5.8k rows per
 // level, warps per SM 2/4/6/8/12/16: 1.708/1.091/0.877/0.765/0.748/0.782 ms;
 // with the L2 prefetch of the next round's metadata, 10 against 12 warps:
 // 0.718 against 0.727 ms, FP32 0.655 against 0.666 ms; the capsp_solve_host
@@ -896,7 +898,7 @@ static void row_shape(capsp_handle_t h, int v, const Tuning &tn, int nrhs, int *
     if (!tn.dflt)
         return;
     if (g == 1) {
-        *block = narrow ? 64 : (wide_levels(h, v) ? 512 : (hostio ? 384 : 320));
+        *block = narrow ? 128 : (wide_levels(h, v) ? 512 : (hostio ? 384 : 320));
         *bps = 1;
     } else if (g == 2) {
         *block = 256;
