@@ -871,10 +871,11 @@ static capsp_status_t ensure_column_order(capsp_handle_t h, int backward)
 // with the L2 prefetch of the next round's metadata, 10 against 12 warps:
 // 0.718 against 0.727 ms, FP32 0.655 against 0.666 ms; the capsp_solve_host
 // build, whose chunks also wait for b and count their rows, keeps 12: 0.742
-// against 0.762 ms) and sixteen the levels of 32k rows and more,
-// which are bound by throughput (2,048 banded systems, 93k rows per level:
-// 2.95 ms at 8, 1.81 ms at 16); with G >= 4 lanes per row a warp holds few
-// rows, so every warp the SM can hold in 128-thread blocks pays off.
+// against 0.762 ms) and every warp the SM holds on levels of 32k rows and
+// more, which are bound by throughput (2,048 banded systems, 93k rows per
+// level: 2.95 ms at 8 warps, 1.77 ms at 16, 1.62 ms at 20 in 128-thread
+// blocks); with G >= 4 lanes per row a warp holds few rows, so there too
+// every warp the SM can hold in 128-thread blocks pays off.
 // Wide levels with G >= 4 lanes per row also take the 64-register kernel build
 // (*cap), whatever the shape.
 // Levels of 32k rows and more on average keep the GPU busy without waiting on
@@ -897,8 +898,11 @@ static void row_shape(capsp_handle_t h, int v, const Tuning &tn, int nrhs, int *
     *bps = tn.bps;
     if (!tn.dflt)
         return;
-    if (g == 1) {
-        *block = narrow ? 128 : (wide_levels(h, v) ? 512 : (hostio ? 384 : 320));
+    if (g == 1 && wide_levels(h, v)) {
+        *block = 128;  // every warp the SM holds
+        *bps = 0;
+    } else if (g == 1) {
+        *block = narrow ? 128 : (hostio ? 384 : 320);
         *bps = 1;
     } else if (g == 2) {
         *block = 256;
