@@ -260,7 +260,10 @@ int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *
         /* cnt[l] now holds the end of level l, cnt[l - 1] its start */
         const int a = cnt[l - 1], b = cnt[l];
         if (b - a > 1) {
+            /* the rows of a level are scattered over the matrix: a wide
+             * level's passes over them run on all host threads */
             int most = 0;
+#pragma omp parallel for schedule(static) reduction(max : most) if (b - a >= 2048)
             for (int k = a; k < b; ++k) {
                 const int i = order[k];
                 const int d = ptr[i + 1] - ptr[i] - 1;
@@ -278,6 +281,7 @@ int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *
                 const int base = cnt[l - 2];
                 range = by_count ? 64 : most > CAPSP_ROW_PASS ? 64 + (a - base) : a - base;
                 const int off = most > CAPSP_ROW_PASS ? 64 : 0;
+#pragma omp parallel for schedule(static) if (b - a >= 2048)
                 for (int k = a; k < b; ++k) {
                     const int i = order[k];
                     const int d = ptr[i + 1] - ptr[i] - 1;
@@ -306,6 +310,7 @@ int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *
                 memcpy(order + a, tmp + a, sizeof(int) * (size_t)(b - a));
             }
         }
+#pragma omp parallel for schedule(static) if (b - a >= 2048)
         for (int k = a; k < b; ++k)
             position[order[k]] = k;
     }
@@ -386,9 +391,28 @@ int capsp_validate(int n, int nnz, const int *ptr, const int *idx, int format, i
         return -1;
     }
     const int diag_last = (format == CAPSP_FMT_CSR) == (uplo == CAPSP_LOWER);
+    /* Rows are checked in parallel for the first bad one (each row checks its
+     * own pointers before it reads idx), then that row again, serially, for
+     * the message. */
+    int first_bad = n;
+#pragma omp parallel for schedule(static, 16384) reduction(min : first_bad)
     for (int i = 0; i < n; ++i) {
         const int s = ptr[i], e = ptr[i + 1];
-        if (e <= s || e > nnz) {
+        int bad = s < 0 || e <= s || e > nnz;
+        if (!bad) {
+            const int dpos = diag_last ? e - 1 : s;
+            bad = idx[dpos] != i;
+            for (int j = s; j < e && !bad; ++j) {
+                const int c = idx[j];
+                bad = j != dpos && !(diag_last ? (c >= 0 && c < i) : (c > i && c < n));
+            }
+        }
+        if (bad && i < first_bad)
+            first_bad = i;
+    }
+    for (int i = first_bad; i < n; ++i) {
+        const int s = ptr[i], e = ptr[i + 1];
+        if (s < 0 || e <= s || e > nnz) {
             snprintf(msg, (size_t)msg_len, "row/column %d is empty or its pointer is out of order", i);
             return -(i + 2);
         }
