@@ -4,6 +4,7 @@ contracts (golden vectors from the reference itself), structure checks."""
 from __future__ import annotations
 
 import ctypes as C
+import os
 import re
 from pathlib import Path
 
@@ -313,3 +314,29 @@ def test_cli_usage_and_degenerate_matrix(tmp_path):
     r = subprocess.run([str(B.CLI), "--out", str(out), str(p)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0
     assert out.exists() and out.read_text() == ""
+
+
+def test_level_schedule_same_on_one_thread():
+    """The parallel per-level passes give the order and positions of a
+    single-threaded build (levels of 2k rows and more run in parallel)."""
+    import hashlib, subprocess, sys, textwrap
+    code = textwrap.dedent("""
+        import hashlib, numpy as np, capellinisptrsv_gb300 as cs
+        from capellinisptrsv_gb300.solver import level_schedule
+        m = cs.generate(n=400_000, kmin=1, kmax=12, band=200_000, seed=21)  # 53 levels of 2k+ rows
+        for upper in (False, True):
+            rp, ci = m.rowptr, m.colidx
+            if upper:
+                rp, ci, _ = cs.matrix_transposition(m.n, m.n, m.nnz, m.rowptr, m.colidx, m.val)
+            _, order, pos, _ = level_schedule(m.n, rp, ci, upper)
+            print(hashlib.sha1(order.tobytes() + pos.tobytes()).hexdigest())
+    """)
+    root = Path(__file__).resolve().parents[1]
+    env = dict(os.environ, PYTHONPATH=str(root))
+    outs = []
+    for threads in ("1", "8"):
+        env["OMP_NUM_THREADS"] = threads
+        r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr
+        outs.append(r.stdout.split())
+    assert outs[0] == outs[1] and len(outs[0]) == 2
