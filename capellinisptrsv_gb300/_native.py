@@ -123,6 +123,7 @@ _SIGS = {
     "capsp_indegree": (None, [I, I, P, P]),
     "capsp_level_schedule": (I, [I, P, P, I, P, P, P]),
     "capsp_level_layout": (I, [I, P, P, I, P, P, P, P, P, P]),
+    "capsp_transpose_structure": (I, [I, I, P, P, P, P, P]),
     "capsp_validate": (I, [I, I, P, P, I, I, C.c_char_p, I]),
     "read_mtx_f64": (I, [C.c_char_p, IP, IP, IP, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
     "read_mtx_f32": (I, [C.c_char_p, IP, IP, IP, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),

@@ -318,23 +318,11 @@ static bool view_level(capsp_handle_t h, int v) { return v == 1 || h->sched == C
 static capsp_status_t transpose_structure(int n, int nnz, const int *ptr, const int *idx, std::vector<int> &tptr,
                                           std::vector<int> &tidx, std::vector<int> &src)
 {
-    tptr.assign((size_t)n + 1, 0);
+    tptr.resize((size_t)n + 1);
     tidx.resize((size_t)nnz);
     src.resize((size_t)nnz);
-    for (int k = 0; k < nnz; ++k) {
-        if (idx[k] < 0 || idx[k] >= n)
-            return fail(CAPSP_ERR_INVALID, "index %d of entry %d is outside [0, %d)", idx[k], k, n);
-        ++tptr[(size_t)idx[k] + 1];
-    }
-    for (int j = 0; j < n; ++j)
-        tptr[(size_t)j + 1] += tptr[(size_t)j];
-    std::vector<int> fill(tptr.begin(), tptr.end() - 1);
-    for (int i = 0; i < n; ++i)
-        for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
-            const int p = fill[(size_t)idx[k]]++;
-            tidx[(size_t)p] = i;
-            src[(size_t)p] = k;
-        }
+    if (capsp_transpose_structure(n, nnz, ptr, idx, tptr.data(), tidx.data(), src.data()) != 0)
+        return fail(CAPSP_ERR_INVALID, "an index is outside [0, %d), or host memory ran out", n);
     return CAPSP_OK;
 }
 

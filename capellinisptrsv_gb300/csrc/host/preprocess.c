@@ -321,6 +321,81 @@ int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *
     return deepest;
 }
 
+static int cmp_u64(const void *x, const void *y)
+{
+    const unsigned long long a = *(const unsigned long long *)x, b = *(const unsigned long long *)y;
+    return a < b ? -1 : a > b ? 1 : 0;
+}
+
+/* The transpose by a counting sort: a histogram of idx, its scan, a scatter
+ * of (row, stored index) pairs into the new rows, then each new row sorted by
+ * row.  The histogram and the scatter take atomic slots in parallel; the sort
+ * restores the stored-row order (rows are distinct within a new row), so the
+ * result is the serial stable one whatever the thread count. */
+int capsp_transpose_structure(int n, int nnz, const int *ptr, const int *idx, int *tptr, int *tidx,
+                              int *src)
+{
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int k = 0; k < nnz; ++k)
+        bad |= idx[k] < 0 || idx[k] >= n;
+    if (bad)
+        return -1;
+    memset(tptr, 0, sizeof(int) * ((size_t)n + 1));
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < nnz; ++k)
+        __atomic_fetch_add(&tptr[idx[k] + 1], 1, __ATOMIC_RELAXED);
+    for (int j = 0; j < n; ++j)
+        tptr[j + 1] += tptr[j];
+    int *fill = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    if (!fill)
+        return -1;
+    memcpy(fill, tptr, sizeof(int) * (size_t)n);
+#pragma omp parallel for schedule(static, 4096)
+    for (int i = 0; i < n; ++i)
+        for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+            const int p = __atomic_fetch_add(&fill[idx[k]], 1, __ATOMIC_RELAXED);
+            tidx[p] = i;
+            src[p] = k;
+        }
+    free(fill);
+    int failed = 0;
+#pragma omp parallel for schedule(dynamic, 4096) reduction(| : failed)
+    for (int j = 0; j < n; ++j) {
+        const int a = tptr[j], e = tptr[j + 1];
+        if (e - a <= 32) {
+            for (int p = a + 1; p < e; ++p) { /* insertion sort by row */
+                const int r = tidx[p], k = src[p];
+                int q = p - 1;
+                while (q >= a && tidx[q] > r) {
+                    tidx[q + 1] = tidx[q];
+                    src[q + 1] = src[q];
+                    --q;
+                }
+                tidx[q + 1] = r;
+                src[q + 1] = k;
+            }
+            continue;
+        }
+        /* a long new row (a heavily referenced index): (row, stored index)
+         * packed into one key, sorted in O(m log m) */
+        unsigned long long *key = (unsigned long long *)malloc(sizeof(unsigned long long) * (size_t)(e - a));
+        if (!key) {
+            failed = 1;
+            continue;
+        }
+        for (int p = a; p < e; ++p)
+            key[p - a] = ((unsigned long long)(unsigned)tidx[p] << 32) | (unsigned)src[p];
+        qsort(key, (size_t)(e - a), sizeof(unsigned long long), cmp_u64);
+        for (int p = a; p < e; ++p) {
+            tidx[p] = (int)(key[p - a] >> 32);
+            src[p] = (int)(key[p - a] & 0xffffffffull);
+        }
+        free(key);
+    }
+    return failed ? -1 : 0;
+}
+
 /* Dependency structure in schedule-position space: for position k (row
  * order[k]) its dependencies' positions, ascending, in dep_idx[dep_ptr[k] ..
  * dep_ptr[k+1]); dep_src gives the index of each dependency's value in the

@@ -552,6 +552,20 @@ def level_layout(n, rowptr, colidx, order, position, upper: bool = False):
     return dep_ptr, dep_idx[:nd], dep_src[:nd], diag_src
 
 
+def transpose_structure(n, rowptr, colidx):
+    """The structure transposed -> (tptr, tidx, src): new row j lists the stored
+    rows holding index j, ascending; src maps new entries to stored ones."""
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    colidx = np.ascontiguousarray(colidx, np.int32)
+    nnz = len(colidx)
+    tptr = np.empty(n + 1, np.int32)
+    tidx = np.empty(max(nnz, 1), np.int32)
+    src = np.empty(max(nnz, 1), np.int32)
+    if N.lib.capsp_transpose_structure(int(n), nnz, _ptr(rowptr), _ptr(colidx), _ptr(tptr), _ptr(tidx), _ptr(src)) != 0:
+        raise ValueError("an index is outside [0, n), or host memory ran out")
+    return tptr, tidx[:nnz], src[:nnz]
+
+
 def matrix_transposition(m, n, nnz, rowptr, colidx, val):
     """CSR -> CSC -> (cscColPtr, cscRowIdx, cscVal)."""
     val = np.ascontiguousarray(val)

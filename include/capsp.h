@@ -457,11 +457,20 @@ int capsp_mix_table(int n, const int *rowptr, int upper, int group_rows, int bor
  * (rows 0..n-1 with the diagonal last, or with upper != 0 rows n-1..0 with the
  * diagonal first): level = 1 + deepest dependency level (the recurrence of
  * matrix_layer); order[k] = k-th row of a sort by level and, inside a level,
- * by dependency count, most first (ties in solve order); position = its
- * inverse; level_start (optional, n+2 ints) = first position of each level.
- * Returns the level count or -1. */
+ * the rows of more than 8 dependencies first by count (most first), then the
+ * others by the position of their newest dependency (a level of 32k rows or
+ * more that holds such a row: by count alone), ties in solve order;
+ * position = its inverse; level_start (optional, n+2 ints) = first position
+ * of each level.  Returns the level count or -1. */
 int capsp_level_schedule(int n, const int *ptr, const int *idx, int upper, int *order,
                          int *position, int *level_start);
+
+/* The structure transposed: new row j lists the stored rows i that hold index
+ * j, ascending; src[p] is the stored index of new entry p.  tptr: n+1; tidx,
+ * src: nnz.  Runs on all host threads; the result does not depend on their
+ * number.  Returns 0, or -1 when an index is outside [0, n). */
+int capsp_transpose_structure(int n, int nnz, const int *ptr, const int *idx, int *tptr, int *tidx,
+                              int *src);
 
 /* Dependencies of every schedule position as positions (ascending), with the
  * source index of each dependency value (dep_src) and of each diagonal

@@ -318,11 +318,12 @@ def test_cli_usage_and_degenerate_matrix(tmp_path):
 
 def test_level_schedule_same_on_one_thread():
     """The parallel per-level passes give the order and positions of a
-    single-threaded build (levels of 2k rows and more run in parallel)."""
+    single-threaded build (levels of 2k rows and more run in parallel), and the
+    threaded transpose its serial result."""
     import hashlib, subprocess, sys, textwrap
     code = textwrap.dedent("""
         import hashlib, numpy as np, capellinisptrsv_gb300 as cs
-        from capellinisptrsv_gb300.solver import level_schedule
+        from capellinisptrsv_gb300.solver import level_schedule, transpose_structure
         m = cs.generate(n=400_000, kmin=1, kmax=12, band=200_000, seed=21)  # 53 levels of 2k+ rows
         for upper in (False, True):
             rp, ci = m.rowptr, m.colidx
@@ -330,6 +331,8 @@ def test_level_schedule_same_on_one_thread():
                 rp, ci, _ = cs.matrix_transposition(m.n, m.n, m.nnz, m.rowptr, m.colidx, m.val)
             _, order, pos, _ = level_schedule(m.n, rp, ci, upper)
             print(hashlib.sha1(order.tobytes() + pos.tobytes()).hexdigest())
+        t = transpose_structure(m.n, m.rowptr, m.colidx)
+        print(hashlib.sha1(b"".join(a.tobytes() for a in t)).hexdigest())
     """)
     root = Path(__file__).resolve().parents[1]
     env = dict(os.environ, PYTHONPATH=str(root))
@@ -339,4 +342,35 @@ def test_level_schedule_same_on_one_thread():
         r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
         assert r.returncode == 0, r.stderr
         outs.append(r.stdout.split())
-    assert outs[0] == outs[1] and len(outs[0]) == 2
+    assert outs[0] == outs[1] and len(outs[0]) == 3
+
+
+def test_transpose_structure_against_scipy():
+    """The host transpose behind the transposed view: new rows in stored-row
+    order, src mapping back to the stored entries, on a band matrix and on one
+    where every row references row 0 (a 50,000-entry new row)."""
+    sp = pytest.importorskip("scipy.sparse")
+    from capellinisptrsv_gb300.solver import transpose_structure
+    m = cs.generate(n=50_000, kmin=1, kmax=9, band=2_000, seed=31)
+    rp, ci = m.rowptr.astype(np.int64), m.colidx.astype(np.int64)
+    heavy_ci = ci.copy()
+    first = rp[:-1][np.diff(rp) > 1]  # first stored entry of every row with an off-diagonal
+    heavy_ci[first] = 0
+    heavy = sp.csr_matrix((np.ones(len(ci)), heavy_ci, rp), shape=(m.n, m.n))
+    heavy.sum_duplicates()
+    heavy.sort_indices()
+    for rows, cols in ((rp, ci), (heavy.indptr.astype(np.int64), heavy.indices.astype(np.int64))):
+        n = len(rows) - 1
+        tptr, tidx, src = transpose_structure(n, rows, cols)
+        ref = sp.csr_matrix((np.arange(len(cols), dtype=np.float64), cols, rows), shape=(n, n)).T.tocsr()
+        ref.sort_indices()
+        assert np.array_equal(tptr, ref.indptr) and np.array_equal(tidx, ref.indices)
+        assert np.array_equal(src, ref.data.astype(np.int64))
+        assert np.array_equal(np.asarray(cols)[src], np.repeat(np.arange(n), np.diff(tptr)))
+    assert np.diff(tptr).max() > 30_000
+
+
+def test_transpose_structure_rejects_bad_index():
+    from capellinisptrsv_gb300.solver import transpose_structure
+    with pytest.raises(ValueError):
+        transpose_structure(3, np.array([0, 1, 3, 5]), np.array([0, 0, 1, 7, 2]))
